@@ -1,0 +1,250 @@
+/*
+ * nbgb.h -- C ABI of the GB300 (sm_103a) force-and-integrate library.
+ *
+ * This is the drop-in boundary for the reference's `include/nbody` hot path.
+ * Every entry point cites the reference interface it replaces (paths are
+ * relative to the reference project root).  Plain C types only: device
+ * pointers are `float*` in the caller's address space, streams are
+ * `cudaStream_t` passed as `void*` (NULL = the library's own stream), and no
+ * C++ exception crosses this boundary -- every call returns an nbgb_status
+ * and leaves a message in nbgb_last_error().  A C++ adapter that rethrows the
+ * reference's exception types is shown in INTEGRATION.md.
+ *
+ * Threading: a calculator, system or ensemble handle must be used by one
+ * host thread at a time (the reference's ParticleSystem is documented "Not
+ * thread-safe", include/nbody/particle_system.hpp:13).  Distinct handles may
+ * be used concurrently from different threads.
+ */
+#ifndef NBGB_H
+#define NBGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBGB_ABI_VERSION 1
+
+/* Status codes.  The C++ adapter maps them to the reference's exceptions
+ * (include/nbody/error_handling.hpp): INVALID_ARG -> ValidationException
+ * (:98-102), OOM -> ResourceException (:76-95), CUDA -> CudaException
+ * (:29-51), OVERFLOW -> std::runtime_error as thrown for an oversize grid
+ * (src/cuda/force_spatial_hash.cu:258-260). */
+typedef enum nbgb_status {
+  NBGB_OK = 0,
+  NBGB_ERR_INVALID_ARG = 1,
+  NBGB_ERR_OOM = 2,
+  NBGB_ERR_CUDA = 3,
+  NBGB_ERR_DEVICE_TIMEOUT = 4, /* a bounded device-side wait gave up */
+  NBGB_ERR_OVERFLOW = 5,       /* grid above 1e8 cells, or a capacity the device exceeded */
+  NBGB_ERR_NOT_READY = 6,      /* asynchronous result not available yet */
+  NBGB_ERR_NO_DEVICE = 7
+} nbgb_status;
+
+/* == nbody::ForceMethod (include/nbody/types.hpp:35), same numeric values,
+ * which are also the values stored in the checkpoint header. */
+typedef enum nbgb_method {
+  NBGB_DIRECT_N2 = 0,
+  NBGB_BARNES_HUT = 1,
+  NBGB_SPATIAL_HASH = 2
+} nbgb_method;
+
+/* == nbody::ParticleData (include/nbody/types.hpp:96-131): 13 separate FP32
+ * arrays and a count, same member order, so a `nbody::ParticleData*` can be
+ * passed where a `nbgb_particle_data*` is expected. */
+typedef struct nbgb_particle_data {
+  float* pos_x;
+  float* pos_y;
+  float* pos_z;
+  float* vel_x;
+  float* vel_y;
+  float* vel_z;
+  float* acc_x;
+  float* acc_y;
+  float* acc_z;
+  float* acc_old_x;
+  float* acc_old_y;
+  float* acc_old_z;
+  float* mass;
+  size_t count;
+} nbgb_particle_data;
+
+/* Parameters of a force calculator.  Defaults (nbgb_params_default) are the
+ * reference's SimulationConfig defaults (include/nbody/types.hpp:133-144)
+ * and ForceCalculator members (include/nbody/force_calculator.hpp:22-25). */
+typedef struct nbgb_params {
+  float G;                /* ForceCalculator::setGravitationalConstant (force_calculator.hpp:19) */
+  float softening;        /* ForceCalculator::setSofteningParameter (:15-18); eps^2 derived */
+  float theta;            /* BarnesHutCalculator(theta), setTheta (:43,47) */
+  float cell_size;        /* SpatialHashCalculator(cell_size, cutoff), setCellSize (:60,64) */
+  float cutoff;           /* setCutoffRadius (:65) */
+  int32_t block_size;     /* DirectForceCalculator(block_size) (:31); accepted, the
+                             library chooses its own tiling */
+  int32_t leaf_capacity;  /* Barnes-Hut bucket size: 1 = the reference tree and walk
+                             (one body per leaf); 2..16 = subtrees with at most this
+                             many bodies are summed body by body when opened */
+  uint32_t flags;         /* NBGB_FLAG_* */
+} nbgb_params;
+
+/* Synchronize the calculator's stream at the end of each call and report any
+ * device-side error word (reference semantics: callers read results right
+ * after computeForces).  Clear it to enqueue asynchronously and check with
+ * nbgb_calculator_synchronize(). */
+#define NBGB_FLAG_SYNC 0x1u
+/* Per-target compensated (two-sum) accumulation across j-tiles.  Clear it
+ * for the plain FP32 sum (one running FP32 accumulator, as the reference). */
+#define NBGB_FLAG_COMPENSATED 0x2u
+/* Record per-target accepted-interaction counts (Barnes-Hut) or neighbour
+ * counts (spatial hash) for nbgb_copy_interaction_counts(). */
+#define NBGB_FLAG_COUNT_INTERACTIONS 0x4u
+
+void nbgb_params_default(nbgb_params* p);
+
+/* ---------------------------------------------------------------------------
+ * Force calculators: nbody::ForceCalculator and its three subclasses
+ * (include/nbody/force_calculator.hpp:8-74) and the factory
+ * createForceCalculator (:76-77, body src/cuda/force_spatial_hash.cu:391-404).
+ * ------------------------------------------------------------------------- */
+typedef struct nbgb_calculator nbgb_calculator;
+
+nbgb_status nbgb_calculator_create(nbgb_method method, const nbgb_params* params,
+                                   nbgb_calculator** out);
+nbgb_status nbgb_calculator_destroy(nbgb_calculator* calc);
+nbgb_status nbgb_calculator_set_params(nbgb_calculator* calc, const nbgb_params* params);
+nbgb_status nbgb_calculator_get_params(const nbgb_calculator* calc, nbgb_params* params);
+/* ForceCalculator::getMethod (force_calculator.hpp:13) */
+nbgb_status nbgb_calculator_get_method(const nbgb_calculator* calc, nbgb_method* method);
+/* All work of the calculator is enqueued on this stream (NULL: a stream the
+ * library creates for the calculator). */
+nbgb_status nbgb_calculator_set_stream(nbgb_calculator* calc, void* cuda_stream);
+/* Waits for the calculator's stream and reports device-side error words. */
+nbgb_status nbgb_calculator_synchronize(nbgb_calculator* calc);
+
+/* ForceCalculator::computeForces (force_calculator.hpp:12; direct
+ * src/cuda/force_direct.cu:103-106, Barnes-Hut force_barnes_hut.cu:577-583,
+ * spatial hash force_spatial_hash.cu:376-388).  Reads pos_x/y/z and mass,
+ * OVERWRITES acc_x/y/z, touches nothing else.  Device pointers. */
+nbgb_status nbgb_compute_forces(nbgb_calculator* calc, const nbgb_particle_data* d_particles);
+
+/* ---------------------------------------------------------------------------
+ * Integrator (include/nbody/integrator.hpp:15-33, src/cuda/integrator.cu).
+ * FP32 SoA semantics of the reference; device pointers.
+ * ------------------------------------------------------------------------- */
+/* Integrator::integrate (integrator.cu:175-189): a_old = a; x += v dt +
+ * a dt^2/2; a = F(x) via calc; v += (a_old + a) dt/2.  Runs on calc's stream. */
+nbgb_status nbgb_integrate(nbgb_calculator* calc, const nbgb_particle_data* d_particles, float dt);
+/* Integrator::updatePositions / updateVelocities / storeOldAccelerations
+ * (integrator.cu:191-201). */
+nbgb_status nbgb_update_positions(const nbgb_particle_data* d_particles, float dt, void* stream);
+nbgb_status nbgb_update_velocities(const nbgb_particle_data* d_particles, float dt, void* stream);
+nbgb_status nbgb_store_old_accelerations(const nbgb_particle_data* d_particles, void* stream);
+/* Integrator::computeKineticEnergy / computePotentialEnergy
+ * (integrator.cu:203-240), reduced in FP64 and returned as double (the
+ * reference returns the FP32 sum of per-block FP32 partials).  Synchronous. */
+nbgb_status nbgb_kinetic_energy(const nbgb_particle_data* d_particles, double* ke, void* stream);
+nbgb_status nbgb_potential_energy(const nbgb_particle_data* d_particles, float G, float eps,
+                                  double* pe, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * ParticleDataManager (include/nbody/particle_data.hpp:9-28,
+ * src/cuda/particle_init.cu:11-160): 13 separate device arrays, acc and
+ * acc_old zeroed; copies move pos, vel, acc and mass (not acc_old), as the
+ * reference does (particle_init.cu:134-160).
+ * ------------------------------------------------------------------------- */
+nbgb_status nbgb_particles_alloc_device(nbgb_particle_data* d, size_t count);
+nbgb_status nbgb_particles_free_device(nbgb_particle_data* d);
+nbgb_status nbgb_particles_copy_to_device(nbgb_particle_data* d, const nbgb_particle_data* h);
+nbgb_status nbgb_particles_copy_to_host(nbgb_particle_data* h, const nbgb_particle_data* d);
+
+/* ---------------------------------------------------------------------------
+ * Inspection for parity tests: what the reference exposes through
+ * BarnesHutTree (include/nbody/barnes_hut_tree.hpp:38-91) and SpatialHashGrid
+ * (include/nbody/spatial_hash_grid.hpp:9-62).  Host output buffers; each call
+ * synchronizes.  Valid after the calculator's last nbgb_compute_forces.
+ * ------------------------------------------------------------------------- */
+
+/* == nbody::OctreeNode (include/nbody/barnes_hut_tree.hpp:9-30), 76 bytes. */
+typedef struct nbgb_octree_node {
+  float center[3];
+  float half_size;
+  float center_of_mass[3];
+  float total_mass;
+  int32_t children[8];
+  int32_t particle_index;
+  uint8_t is_leaf;
+  uint8_t pad_[3];
+  int32_t particle_count;
+} nbgb_octree_node;
+
+/* BarnesHutTree::getNodeCount / getMaxDepth (barnes_hut_tree.hpp:57-58). */
+nbgb_status nbgb_bh_tree_stats(nbgb_calculator* calc, int32_t* node_count, int32_t* max_depth);
+/* The (Morton key, particle index) pairs after the stable sort
+ * (force_barnes_hut.cu:308-328); n = particle count. */
+nbgb_status nbgb_bh_copy_sorted_keys(nbgb_calculator* calc, uint32_t* keys, int32_t* indices,
+                                     size_t n);
+/* The tree in the reference node layout (BarnesHutTree::copyNodesToHost,
+ * force_barnes_hut.cu:557-560).  Node 0 is the root; nodes are numbered in
+ * depth-first pre-order (the reference numbers in insertion order), children
+ * hold node indices, -1 for empty octants. */
+nbgb_status nbgb_bh_copy_nodes(nbgb_calculator* calc, nbgb_octree_node* nodes, size_t capacity);
+/* SpatialHashGrid::getGridDims / getCellSize / getTotalCells
+ * (spatial_hash_grid.hpp:25-27) plus the padded bbox minimum. */
+nbgb_status nbgb_hash_grid_info(nbgb_calculator* calc, int32_t dims[3], float bbox_min[3],
+                                float* cell_size, int64_t* total_cells);
+/* SpatialHashGrid::copyCellDataToHost (force_spatial_hash.cu:324-340).
+ * Within a cell, particles are in ascending index order. */
+nbgb_status nbgb_hash_copy_cells(nbgb_calculator* calc, int32_t* cell_start, int32_t* cell_end,
+                                 int32_t* particle_cells, int32_t* sorted_indices);
+/* Per-target accepted interactions (Barnes-Hut) or neighbours within the
+ * cutoff (spatial hash), recorded under NBGB_FLAG_COUNT_INTERACTIONS. */
+nbgb_status nbgb_copy_interaction_counts(nbgb_calculator* calc, int32_t* counts, size_t n);
+
+/* ---------------------------------------------------------------------------
+ * Device-resident simulation with FP64 position/velocity state: the fast
+ * path under ParticleSystem::update (src/core/particle_system.cpp:122-136).
+ * Kick-drift-kick (algebraically the reference's Velocity Verlet,
+ * src/cuda/integrator.cu:175-189) with x, v in FP64 and FP32 forces.
+ * ------------------------------------------------------------------------- */
+typedef struct nbgb_system nbgb_system;
+
+/* Copies the initial state from HOST arrays (pos, vel, mass of h) and
+ * computes a(0) with calc (ParticleSystem::finishInitialization,
+ * particle_system.cpp:45-61).  The system keeps a reference to calc. */
+nbgb_status nbgb_system_create(nbgb_calculator* calc, const nbgb_particle_data* h_init,
+                               nbgb_system** out);
+nbgb_status nbgb_system_destroy(nbgb_system* sys);
+/* `steps` Velocity-Verlet steps of size dt (ParticleSystem::update x steps). */
+nbgb_status nbgb_system_step(nbgb_system* sys, float dt, int32_t steps);
+/* FP32 view into HOST arrays (pos, vel, acc, mass; acc_old untouched):
+ * ParticleSystem::copyToHost / getState (particle_system.cpp:228-253). */
+nbgb_status nbgb_system_read(nbgb_system* sys, nbgb_particle_data* h_out);
+/* FP64 state into host arrays (any pointer may be NULL). */
+nbgb_status nbgb_system_read_f64(nbgb_system* sys, double* x, double* y, double* z, double* vx,
+                                 double* vy, double* vz);
+/* FP64 energy and momentum: KE = sum m v^2/2, PE = -sum_{i<j} G m_i m_j /
+ * sqrt(r^2 + eps^2) (integrator.cu:52-120), P = sum m v. */
+nbgb_status nbgb_system_energy(nbgb_system* sys, double* ke, double* pe, double momentum[3]);
+
+/* ---------------------------------------------------------------------------
+ * Diagnostics (no reference counterpart): measured FP32 pipe rates of the
+ * current device -- FFMA and packed FFMA2 in TFLOP/s (2 flops per lane-FMA)
+ * and MUFU rsqrt in Gop/s -- used as roofline denominators for the force
+ * kernels.  Synchronous; any pointer may be NULL.
+ * ------------------------------------------------------------------------- */
+nbgb_status nbgb_measure_fp32_peak(double* ffma_tflops, double* ffma2_tflops, double* mufu_gops);
+
+/* ---------------------------------------------------------------------------
+ * Library information.
+ * ------------------------------------------------------------------------- */
+/* Message of the last failing call on this thread ("" if none). */
+const char* nbgb_last_error(void);
+const char* nbgb_version(void);
+int32_t nbgb_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBGB_H */

@@ -1,0 +1,117 @@
+// runtime.cuh -- device buffers and the internal state behind the C handles.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace nbgb {
+
+// Growable device allocation (contents are not preserved on growth).
+template <typename T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t cap = 0;  // elements
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+  T* ensure(size_t n) {
+    if (n <= cap && ptr) return ptr;
+    release();
+    size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&ptr, bytes);
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      cudaGetLastError();
+      char buf[160];
+      std::snprintf(buf, sizeof buf, "device allocation of %zu bytes failed: %s", bytes,
+                    cudaGetErrorString(e));
+      fail(e == cudaErrorMemoryAllocation ? NBGB_ERR_OOM : NBGB_ERR_CUDA, buf);
+    }
+    cap = std::max<size_t>(n, 1);
+    return ptr;
+  }
+  size_t bytes() const { return cap * sizeof(T); }
+};
+
+// Pinned host scalars used to read small device results.
+template <typename T>
+struct HostPinned {
+  T* ptr = nullptr;
+  size_t n = 0;
+  HostPinned() = default;
+  HostPinned(const HostPinned&) = delete;
+  HostPinned& operator=(const HostPinned&) = delete;
+  ~HostPinned() {
+    if (ptr) cudaFreeHost(ptr);
+  }
+  T* ensure(size_t k) {
+    if (k <= n && ptr) return ptr;
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    NBGB_CUDA(cudaMallocHost(&ptr, std::max<size_t>(k, 1) * sizeof(T)));
+    n = std::max<size_t>(k, 1);
+    return ptr;
+  }
+};
+
+struct BHState;    // bh.cu
+struct HashState;  // hash.cu
+void bh_state_delete(BHState*);
+void hash_state_delete(HashState*);
+
+struct BHDeleter {
+  void operator()(BHState* p) const { bh_state_delete(p); }
+};
+struct HashDeleter {
+  void operator()(HashState* p) const { hash_state_delete(p); }
+};
+
+}  // namespace nbgb
+
+struct nbgb_calculator {
+  nbgb_method method = NBGB_DIRECT_N2;
+  nbgb_params params{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int device = 0;
+  nbgb::DirectVariant variant = nbgb::DirectVariant::kScalar4;
+
+  nbgb::DevBuf<float4> pm;        // packed (x, y, z, m) input of the last drop-in call
+  nbgb::DevBuf<float4> partial;   // direct j-split partials
+  nbgb::DevBuf<uint32_t> err;     // device error word
+  nbgb::DevBuf<int32_t> counts;   // per-target interaction / neighbour counts
+  nbgb::DevBuf<double> red;       // reduction partials
+  nbgb::HostPinned<uint32_t> h_err;
+  nbgb::HostPinned<double> h_red;
+  int64_t last_n = 0;
+
+  std::unique_ptr<nbgb::BHState, nbgb::BHDeleter> bh;
+  std::unique_ptr<nbgb::HashState, nbgb::HashDeleter> hash;
+};
+
+namespace nbgb {
+
+// Forces on n bodies given as packed float4 `pm` (padded by the callee's own
+// requirements where needed); writes ax/ay/az (length n).  Enqueued on
+// calc->stream.  Defined in api.cu; the method backends live in bh.cu and
+// hash.cu.
+void forces_packed(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float* ay,
+                   float* az);
+void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float* ay, float* az);
+void hash_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float* ay,
+                 float* az);
+// Sources padded for the direct kernel: returns the padded length.
+int64_t direct_pad(int64_t n);
+// Wait for the calculator's stream and turn device error bits into an Error.
+void check_device_errors(nbgb_calculator* c);
+
+}  // namespace nbgb

@@ -1,0 +1,98 @@
+"""Build recipe for the parity checker (test infrastructure only).
+
+* ``oracle/liboracle.so``: the C restatement in ``nbody_oracle.c``, built with
+  ``-ffp-contract=off`` (see that file's header) and OpenMP.
+* ``oracle/_ref/libnbody_ref.so``: the reference's own host-side code,
+  compiled in place from the reference sources plus ``ref_harness.cpp``.  Only
+  built where the reference tree exists; outputs go to ``oracle/_ref/`` only.
+
+Usage: ``python oracle/build.py [--ref]``.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_ROOT = os.environ.get("NBGB_REFERENCE_ROOT", "/root/reference")
+LIB = os.path.join(HERE, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_LIB = os.path.join(REF_DIR, "libnbody_ref.so")
+
+# Reference sources whose host code the harness drives (relative to the
+# reference root).  They are compiled where they lie; nothing is copied.
+_REF_CU = ["src/cuda/force_direct.cu", "src/cuda/force_barnes_hut.cu",
+           "src/cuda/force_spatial_hash.cu", "src/cuda/particle_init.cu"]
+_REF_CPP = ["src/utils/error_handling.cpp", "src/utils/performance_observability.cpp",
+            "src/utils/serialization.cpp", "src/utils/simulation_state.cpp"]
+_REF_DEFS = ["-DNDEBUG", "-DNBODY_WITH_CUDA=1", "-DNBODY_WITH_RENDERING=0",
+             "-DNBODY_WITH_UI=0", "-DNBODY_ENABLE_PROFILING=0"]
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
+
+
+def _stale(out: str, srcs: list[str]) -> bool:
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(s) > t for s in srcs)
+
+
+def build_oracle(force: bool = False) -> str:
+    src = os.path.join(HERE, "nbody_oracle.c")
+    if force or _stale(LIB, [src]):
+        tmp = LIB + ".tmp"
+        _run(["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-shared",
+              "-fPIC", "-std=c11", src, "-o", tmp, "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def reference_available() -> bool:
+    return os.path.isfile(os.path.join(REF_ROOT, "src/cuda/force_barnes_hut.cu"))
+
+
+def build_ref(force: bool = False) -> str | None:
+    """Compile the reference host code + harness into oracle/_ref (CPU use only)."""
+    if not reference_available():
+        return None
+    harness = os.path.join(HERE, "ref_harness.cpp")
+    srcs = [os.path.join(REF_ROOT, s) for s in _REF_CU + _REF_CPP] + [harness]
+    if not (force or _stale(REF_LIB, srcs)):
+        return REF_LIB
+    os.makedirs(REF_DIR, exist_ok=True)
+    inc = ["-I", os.path.join(REF_ROOT, "include")]
+    # The reference is built with separable compilation (its CMakeLists sets
+    # CUDA_SEPARABLE_COMPILATION); the kernels are compiled but never run here.
+    nv = ["nvcc", "-std=c++17", "-O3", "-rdc=true", "-Xcompiler", "-fPIC",
+          "-gencode", "arch=compute_103a,code=sm_103a"] + _REF_DEFS + inc
+    gx = ["g++", "-std=c++17", "-O3", "-fPIC", "-I", "/usr/local/cuda/include"] + _REF_DEFS + inc
+    jobs, objs = [], []
+    for s in _REF_CU:
+        o = os.path.join(REF_DIR, os.path.basename(s) + ".o")
+        jobs.append(nv + ["-c", os.path.join(REF_ROOT, s), "-o", o])
+        objs.append(o)
+    for s in _REF_CPP:
+        o = os.path.join(REF_DIR, os.path.basename(s) + ".o")
+        jobs.append(gx + ["-c", os.path.join(REF_ROOT, s), "-o", o])
+        objs.append(o)
+    ho = os.path.join(REF_DIR, "ref_harness.o")
+    jobs.append(gx + ["-c", harness, "-o", ho])
+    objs.append(ho)
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        list(ex.map(_run, jobs))
+    _run(["nvcc", "-shared", "-rdc=true", "-gencode", "arch=compute_103a,code=sm_103a",
+          "-cudart", "shared", "-Xlinker", "-Bsymbolic", *objs, "-o", REF_LIB])
+    return REF_LIB
+
+
+if __name__ == "__main__":
+    print(build_oracle(force=True))
+    if "--ref" in sys.argv:
+        print(build_ref(force=True))

@@ -1,0 +1,158 @@
+"""Velocity Verlet through the C ABI vs the oracle (GPU).
+
+Restates tests/test_integrator.cpp and checks trajectories of the Plummer
+N = 1024 direct workload (100 steps, dt = 1e-3, eps = 0.01):
+  * FP32 drop-in path vs the oracle's FP32 reference-formula integration:
+    max |x - x_oracle| <= 1e-4;
+  * FP64-state system path vs the FP64 oracle: max |x - x64| <= 2e-5 and
+    |v - v64| <= 2e-4, energy drift |dE/E| <= 1e-5.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _one(v):
+    return np.array([v], np.float32)
+
+
+def test_single_step_position(nb):
+    # tests/test_integrator.cpp:14-41
+    with nb.ScopedParticleData(1, {"vel_x": _one(1.0), "mass": _one(1.0)}) as p:
+        nb.Integrator().updatePositions(p.device, 0.1)
+        p.download()
+        assert abs(p.host["pos_x"][0] - 0.1) < 1e-5
+        assert abs(p.host["pos_y"][0]) < 1e-5 and abs(p.host["pos_z"][0]) < 1e-5
+
+
+def test_constant_acceleration_kinematics(nb):
+    # :43-74
+    arr = {"pos_x": _one(1.0), "pos_y": _one(-2.0), "pos_z": _one(0.5), "vel_x": _one(0.3),
+           "vel_z": _one(-0.2), "acc_x": _one(2.0), "acc_y": _one(-1.0), "acc_z": _one(4.0),
+           "mass": _one(1.0)}
+    with nb.ScopedParticleData(1, arr) as p:
+        dt = 0.01
+        nb.Integrator().updatePositions(p.device, dt)
+        p.download()
+        h = p.host
+        assert abs(h["pos_x"][0] - (1.0 + 0.3 * dt + 0.5 * 2.0 * dt * dt)) < 1e-6
+        assert abs(h["pos_y"][0] - (-2.0 - 0.5 * dt * dt)) < 1e-6
+        assert abs(h["pos_z"][0] - (0.5 - 0.2 * dt + 0.5 * 4.0 * dt * dt)) < 1e-6
+
+
+def test_kinetic_energy(nb):
+    # :76-102
+    arr = {"vel_x": np.array([1.0, 0.0], np.float32), "vel_y": np.array([0.0, 2.0], np.float32),
+           "mass": np.array([1.0, 2.0], np.float32)}
+    with nb.ScopedParticleData(2, arr) as p:
+        assert abs(nb.Integrator().computeKineticEnergy(p.device) - 4.5) < 1e-4
+
+
+def _orbit_state():
+    r, G, m = 5.0, 1.0, 1.0
+    v = np.sqrt(G * m / (4 * r))
+    return {"pos_x": np.array([-r, r], np.float32), "vel_y": np.array([-v, v], np.float32),
+            "mass": np.ones(2, np.float32)}
+
+
+def test_two_body_orbit_energy_dropin(nb):
+    # :107-168: r = 5, eps = 0.01, dt = 1e-3, 100 steps, |dE/E| < 1e-3
+    calc = nb.DirectForceCalculator()
+    calc.setGravitationalConstant(1.0)
+    calc.setSofteningParameter(0.01)
+    integ = nb.Integrator()
+    with nb.ScopedParticleData(2, _orbit_state()) as p:
+        calc.computeForces(p.device)
+        e0 = integ.computeTotalEnergy(p.device, 1.0, 0.01)
+        for _ in range(100):
+            integ.integrate(p.device, calc, 0.001)
+        e1 = integ.computeTotalEnergy(p.device, 1.0, 0.01)
+        assert abs(e1 - e0) / abs(e0) < 1e-3
+    calc.close()
+
+
+def test_two_body_orbit_energy_system(nb):
+    st = _orbit_state()
+    s = {"x": st["pos_x"], "y": np.zeros(2, np.float32), "z": np.zeros(2, np.float32),
+         "vx": np.zeros(2, np.float32), "vy": st["vel_y"], "vz": np.zeros(2, np.float32),
+         "m": st["mass"]}
+    calc = nb.DirectForceCalculator()
+    calc.setSofteningParameter(0.01)
+    sysm = nb.System(calc, s)
+    ke0, pe0, p0 = sysm.energy()
+    sysm.step(0.001, 100)
+    ke1, pe1, p1 = sysm.energy()
+    e0, e1 = ke0 + pe0, ke1 + pe1
+    assert abs(e1 - e0) / abs(e0) < 1e-5
+    assert np.all(np.abs(p1 - p0) < 1e-9)
+    sysm.close()
+    calc.close()
+
+
+def test_potential_energy_vs_oracle(nb, orc):
+    s = nb.ics.plummer(2000, seed=9)
+    with nb.ScopedParticleData(2000, {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"],
+                                      "mass": s["m"]}) as p:
+        pe = nb.Integrator().computePotentialEnergy(p.device, 1.0, 0.01)
+    ref = orc.potential_energy(s["x"], s["y"], s["z"], s["m"], 1.0, 0.01)
+    assert abs(pe - ref) / abs(ref) < 1e-6
+
+
+def _c1():
+    return 1024, 0.01, 0.001, 100
+
+
+def test_dropin_trajectory_vs_oracle_fp32(nb, orc):
+    n, eps, dt, steps = _c1()
+    s = nb.ics.plummer(n, seed=1)
+    calc = nb.DirectForceCalculator()
+    calc.setSofteningParameter(eps)
+    integ = nb.Integrator()
+    arr = {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"], "vel_x": s["vx"],
+           "vel_y": s["vy"], "vel_z": s["vz"], "mass": s["m"]}
+    with nb.ScopedParticleData(n, arr) as p:
+        calc.computeForces(p.device)
+        for _ in range(steps):
+            integ.integrate(p.device, calc, dt)
+        p.download()
+        gx, gy, gz = p.host["pos_x"].copy(), p.host["pos_y"].copy(), p.host["pos_z"].copy()
+    calc.close()
+    # oracle: reference formulas in FP32 with the reference-order direct sum
+    x, y, z = s["x"].copy(), s["y"].copy(), s["z"].copy()
+    vx, vy, vz = s["vx"].copy(), s["vy"].copy(), s["vz"].copy()
+    ax, ay, az = orc.direct_f32(x, y, z, s["m"], 1.0, eps)
+    for _ in range(steps):
+        ox, oy, oz = ax.copy(), ay.copy(), az.copy()
+        orc.update_positions(x, y, z, vx, vy, vz, ax, ay, az, dt)
+        ax, ay, az = orc.direct_f32(x, y, z, s["m"], 1.0, eps)
+        orc.update_velocities(vx, vy, vz, ox, oy, oz, ax, ay, az, dt)
+    dev = max(np.abs(gx - x).max(), np.abs(gy - y).max(), np.abs(gz - z).max())
+    assert dev <= 1e-4, dev
+
+
+def test_system_trajectory_vs_fp64(nb, orc):
+    n, eps, dt, steps = _c1()
+    s = nb.ics.plummer(n, seed=1)
+    calc = nb.DirectForceCalculator()
+    calc.setSofteningParameter(eps)
+    sysm = nb.System(calc, s)
+    ke0, pe0, _ = sysm.energy()
+    sysm.step(dt, steps)
+    ke1, pe1, _ = sysm.energy()
+    got = sysm.read_f64()
+    sysm.close()
+    calc.close()
+    st = {k: s[k].astype(np.float64) for k in ("x", "y", "z", "vx", "vy", "vz")}
+    m = s["m"].astype(np.float64)
+    st["ax"], st["ay"], st["az"] = orc.direct_f64(st["x"], st["y"], st["z"], m, 1.0, eps)
+    for _ in range(steps):
+        orc.vv_step_f64(st, m, 1.0, eps, dt)
+    dx = max(np.abs(got[k] - st[k]).max() for k in ("x", "y", "z"))
+    dv = max(np.abs(got[k] - st[k]).max() for k in ("vx", "vy", "vz"))
+    assert dx <= 2e-5, dx
+    assert dv <= 2e-4, dv
+    e0, e1 = ke0 + pe0, ke1 + pe1
+    assert abs(e1 - e0) / abs(e0) <= 1e-5

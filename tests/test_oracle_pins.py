@@ -1,0 +1,192 @@
+"""Pin the CPU oracle to the reference: golden vectors made by the reference's
+own host code (tests/golden/make_golden.py) and the reference's known-answer
+tests.  CPU only."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+
+def test_pair_function_matches_reference_bitwise(orc, golden):
+    g = golden("ref_pair.npz")
+    for j in range(len(g["m2"])):
+        out = orc.pair_accel(g["p1"][j], g["p2"][j], g["m2"][j], g["G"][j], g["eps"][j])
+        np.testing.assert_array_equal(out.view(np.uint32), g["acc"][j].view(np.uint32))
+
+
+def test_pair_known_answers(orc):
+    # tests/test_force_calculation.cpp:17-34: |a| = G m2 / r^2 along +x
+    a = orc.pair_accel([0, 0, 0], [1, 0, 0], 1.0, 1.0, 0.0)
+    assert a[0] > 0 and abs(a[1]) < 1e-6 and abs(a[2]) < 1e-6
+    assert abs(np.linalg.norm(a) - 1.0) < 1e-5
+    # :36-48 softening keeps it finite
+    assert np.all(np.isfinite(orc.pair_accel([0, 0, 0], [0.001, 0, 0], 1.0, 1.0, 0.1)))
+    # :181-204 softened magnitude G m r / (r^2+eps^2)^1.5 within 1%
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        m2, r = rng.uniform(0.01, 100), rng.uniform(0.05, 100)
+        a = orc.pair_accel([0, 0, 0], [r, 0, 0], m2, 1.0, 0.01)
+        exp = m2 * r / (r * r + 1e-4) ** 1.5
+        assert abs(np.linalg.norm(a) - exp) / exp < 0.01
+
+
+def test_morton_codes_match_reference(orc, golden):
+    g = golden("ref_morton.npz")
+    got = np.array([orc.morton_code(*v) for v in g["n"]], np.uint32)
+    np.testing.assert_array_equal(got, g["code"])
+
+
+def test_cell_index_known_answer(golden):
+    # tests/test_spatial_hash.cpp:34-47; getCellIndex = floor(p / cell)
+    g = golden("ref_cells.npz")
+    p, c, idx = g["p"], g["cell"], g["idx"]
+    got = np.floor(p / c[:, None]).astype(np.int32)  # float32 IEEE division, as the kernel
+    np.testing.assert_array_equal(got, idx)
+    assert tuple(idx[-2]) == (1, 2, 3)
+
+
+def _tree_case(golden, name):
+    g = golden("ref_trees.npz")
+    from oracle.oracle import NODE_DTYPE
+    nodes = np.frombuffer(g[f"{name}_nodes"].tobytes(), NODE_DTYPE)
+    return {k: g[f"{name}_{k}"] for k in ("x", "y", "z", "m", "keys", "sorted")}, nodes, \
+        int(g[f"{name}_depth"])
+
+
+@pytest.mark.parametrize("name", ["sph30", "sph100", "sph700", "uni500", "coincident16",
+                                  "collinear16"])
+def test_octree_matches_reference_bitwise(orc, golden, name):
+    s, ref_nodes, ref_depth = _tree_case(golden, name)
+    bmin, bmax = orc.bbox(s["x"], s["y"], s["z"])
+    keys, idx = orc.morton_keys(s["x"], s["y"], s["z"], bmin, bmax)
+    ks, si = orc.stable_sort(keys, idx)
+    np.testing.assert_array_equal(ks, s["keys"])
+    np.testing.assert_array_equal(si, s["sorted"])
+    nodes, depth, _ = orc.build_octree(s["x"], s["y"], s["z"], s["m"], si, bmin, bmax)
+    assert depth == ref_depth
+    assert len(nodes) == len(ref_nodes)
+    assert nodes.tobytes() == ref_nodes.tobytes()
+
+
+def test_octree_mass_conservation(orc, golden):
+    # tests/test_barnes_hut.cpp:34-89: root mass equals the total mass
+    for name in ("sph100", "coincident16", "collinear16"):
+        s, _, _ = _tree_case(golden, name)
+        bmin, bmax = orc.bbox(s["x"], s["y"], s["z"])
+        _, si = orc.stable_sort(*orc.morton_keys(s["x"], s["y"], s["z"], bmin, bmax))
+        nodes, _, _ = orc.build_octree(s["x"], s["y"], s["z"], s["m"], si, bmin, bmax)
+        tot = float(np.sum(s["m"], dtype=np.float32))
+        assert abs(tot - nodes[0]["mass"]) < 1e-3 * tot
+
+
+def test_reference_node_budget_merges_small_systems(orc, golden):
+    # The reference sizes its node array at 2N and stops splitting leaves once
+    # node_count + 33 >= 2N (force_barnes_hut.cu:253,449-453).  For N = 30
+    # that merges 9 bodies into multi-body leaves, and its own theta = 0.1
+    # equivalence test (tests/test_spatial_hash.cpp:171-228) cannot reach 2 %
+    # on that tree.  The CUDA build uses the canonical tree (no budget), which
+    # is the reference tree whenever the budget does not fire (N >~ 64).
+    g = golden("ref_inputs.npz")
+    x, y, z, m = (g[f"sph30_r5_{k}"] for k in ("x", "y", "z", "m"))
+    bmin, bmax = orc.bbox(x, y, z)
+    _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
+    nodes, _, merges = orc.build_octree(x, y, z, m, si, bmin, bmax)
+    assert merges == 9 and len(nodes) == 30
+    dx, dy, dz = orc.direct_f32(x, y, z, m, 1.0, 0.1)
+    bx, _, _, _ = orc.bh_forces(nodes, x, y, z, m, 0.1, 1.0, 0.1)
+    assert rel_err(bx, dx, 1e-4).max() > 0.02
+
+
+def test_bh_small_theta_matches_direct(orc, golden):
+    # tests/test_spatial_hash.cpp:171-228 (theta = 0.1 vs direct, < 2 %), on
+    # the canonical tree (node array large enough that no budget merge fires).
+    g = golden("ref_inputs.npz")
+    x, y, z, m = (g[f"sph30_r5_{k}"] for k in ("x", "y", "z", "m"))
+    dx, dy, dz = orc.direct_f32(x, y, z, m, 1.0, 0.1)
+    bmin, bmax = orc.bbox(x, y, z)
+    _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
+    nodes, _, merges = orc.build_octree(x, y, z, m, si, bmin, bmax, max_nodes=64 * 30 + 64)
+    assert merges == 0
+    bx, by, bz, _ = orc.bh_forces(nodes, x, y, z, m, 0.1, 1.0, 0.1)
+    err = max(rel_err(bx, dx, 1e-4).max(), rel_err(by, dy, 1e-4).max(),
+              rel_err(bz, dz, 1e-4).max())
+    assert err < 0.02
+
+
+def test_bh_theta_convergence(orc, golden):
+    # tests/test_barnes_hut.cpp:168-220
+    g = golden("ref_inputs.npz")
+    x, y, z, m = (g[f"sph50_r10_{k}"] for k in ("x", "y", "z", "m"))
+    dx, dy, dz = orc.direct_f32(x, y, z, m, 1.0, 0.1)
+    bmin, bmax = orc.bbox(x, y, z)
+    _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
+    nodes, _, _ = orc.build_octree(x, y, z, m, si, bmin, bmax, max_nodes=64 * 50 + 64)
+
+    def total(theta):
+        bx, by, bz, _ = orc.bh_forces(nodes, x, y, z, m, theta, 1.0, 0.1)
+        return np.sum(np.sqrt((bx - dx) ** 2 + (by - dy) ** 2 + (bz - dz) ** 2))
+
+    assert total(0.3) <= 1.1 * total(0.8)
+
+
+def test_direct_grid32_self_consistency(orc, golden):
+    # tests/test_force_calculation.cpp:108-148 builds its expectation from the
+    # pair function in ascending j; the oracle's direct sum is that loop.
+    g = golden("ref_inputs.npz")
+    x, y, z, m = g["grid32_x"], g["grid32_y"], g["grid32_z"], g["grid32_m"]
+    ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, 0.1)
+    for i in range(32):
+        ref = np.zeros(3, np.float32)
+        for j in range(32):
+            if i != j:
+                ref += orc.pair_accel([x[i], y[i], z[i]], [x[j], y[j], z[j]], m[j], 1.0, 0.1)
+        np.testing.assert_array_equal(np.array([ax[i], ay[i], az[i]], np.float32), ref)
+
+
+def test_hash_build_partitions_particles(orc, golden):
+    # tests/test_spatial_hash.cpp:133-167: every particle in exactly one cell
+    g = golden("ref_inputs.npz")
+    x, y, z = (g[f"uni50_10_{k}"] for k in ("x", "y", "z"))
+    for cell in (0.6, 1.0, 2.0, 5.5, 9.9):
+        grid = orc.hash_build(x, y, z, cell)
+        seen = np.concatenate([grid["sorted_indices"][s:e] for s, e in
+                               zip(grid["cell_start"], grid["cell_end"])])
+        assert sorted(seen.tolist()) == list(range(50))
+        assert np.all(np.diff(grid["cell_start"]) >= 0)
+
+
+def test_hash_cutoff_boundary(orc):
+    # tests/test_spatial_hash.cpp:81-127
+    G, eps, cutoff, cell = 1.0, 0.01, 2.0, 2.0
+    for r, zero in ((2.25, True), (1.75, False)):
+        x = np.array([0.0, r], np.float32)
+        y = np.zeros(2, np.float32)
+        z = np.zeros(2, np.float32)
+        m = np.ones(2, np.float32)
+        grid = orc.hash_build(x, y, z, cell)
+        ax, ay, az, nbrs = orc.hash_forces(grid, x, y, z, m, cutoff, G, eps)
+        if zero:
+            assert ax[0] == 0.0 and ay[0] == 0.0 and az[0] == 0.0 and ax[1] == 0.0
+            assert nbrs.tolist() == [0, 0]
+        else:
+            d2 = r * r + eps * eps
+            exp = G * r / (d2 * np.sqrt(d2))
+            assert abs(ax[0] - exp) < 1e-4 and abs(ax[1] + exp) < 1e-4
+
+
+def test_integrator_known_answers(orc):
+    # tests/test_integrator.cpp:14-74
+    one = lambda v: np.array([v], np.float32)  # noqa: E731
+    x, y, z = one(0), one(0), one(0)
+    orc.update_positions(x, y, z, one(1), one(0), one(0), one(0), one(0), one(0), 0.1)
+    assert abs(x[0] - 0.1) < 1e-5 and abs(y[0]) < 1e-5
+    x, y, z = one(1.0), one(-2.0), one(0.5)
+    dt = 0.01
+    orc.update_positions(x, y, z, one(0.3), one(0.0), one(-0.2), one(2.0), one(-1.0), one(4.0), dt)
+    assert abs(x[0] - (1.0 + 0.3 * dt + 0.5 * 2.0 * dt * dt)) < 1e-6
+    assert abs(y[0] - (-2.0 - 0.5 * dt * dt)) < 1e-6
+    assert abs(z[0] - (0.5 - 0.2 * dt + 0.5 * 4.0 * dt * dt)) < 1e-6
+    # :76-102 KE = 4.5
+    assert abs(orc.kinetic_energy([1.0, 0.0], [0.0, 2.0], [0.0, 0.0], [1.0, 2.0]) - 4.5) < 1e-12
