@@ -97,7 +97,8 @@ class ParticleData:
         pd = cls(n)
         for f in FIELDS:
             a = arrays.get(f)
-            a = np.zeros(n, np.float32) if a is None else np.ascontiguousarray(a, np.float32)
+            # always a private copy: downloads must never write into caller arrays
+            a = np.zeros(n, np.float32) if a is None else np.array(a, dtype=np.float32, copy=True)
             if len(a) != n:
                 raise ValidationException(f"Validation Error: field {f} has length {len(a)} != {n}")
             pd._keep[f] = a
