@@ -1,0 +1,443 @@
+#!/usr/bin/env python3
+"""Ensemble-serving benchmark on one GB300 (one JSON line on stdout).
+
+Workload (synthetic, seeded): a stream of independent Plummer clusters
+(a = 1, M = 1, G = 1) with N log-uniform in [256, 65536], step counts uniform
+in [100, 2000], eps = 0.01, dt = 1e-3; direct sum for N <= 8192, Barnes-Hut
+theta = 0.5 otherwise; FP32 forces, FP64 x/v state; 64 GiB admission budget.
+
+  value   batched particle-steps/s: `--steps` ticks of the continuous-batching
+          engine at saturation (resident cap `--resident`, backlog queued),
+          timed with CUDA events on the engine stream;
+  plain   the same requests run one at a time through the plain device path
+          (nbgb_system per request), particle-steps/s;
+  serve   Poisson arrivals at 80 % of the measured capacity: p50/p99 request
+          latency (arrival -> result on the host) and e2e particle-steps/s
+          through the public API (host arrays in, host results out).
+
+`--impl reference` times the reference's CPU path for the same workload (the
+CPU restatement in oracle/, all host threads).  Multi-GPU: one replica per
+rank on its own shard of the request stream (weak scaling), max time over
+ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "nbody-gpu-sim_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "batched vs plain particle-steps/s on 1 GB300 at stated force err; p99 latency"
+UNIT = "particle-steps/s"
+WORKLOAD = ("ensemble serving: Plummer clusters (a=1, M=1), N log-uniform [256, 65536], "
+            "steps U[100, 2000], eps=0.01, dt=1e-3, direct N<=8192 else Barnes-Hut theta=0.5, "
+            "FP32 forces + FP64 state, 64 GiB admission budget")
+DT = 1e-3
+EPS = 0.01
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60, help="timed engine ticks")
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="nbgb", choices=["nbgb", "reference"])
+    ap.add_argument("--resident", type=int, default=96, help="resident systems at saturation")
+    ap.add_argument("--plain-requests", type=int, default=48)
+    ap.add_argument("--plain-steps", type=int, default=20)
+    ap.add_argument("--serve-requests", type=int, default=192)
+    ap.add_argument("--serve-max-s", type=float, default=90.0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class Clocks:
+    """nvidia-smi samples every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int) -> None:
+        self.idx = gpu_index
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            if self.thread:
+                self.thread.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def make_state(nbgb, req):
+    return nbgb.ics.plummer(req["n"], seed=req["seed"])
+
+
+def request_work(reqs) -> float:
+    return float(sum(r["n"] * r["steps"] for r in reqs))
+
+
+# ----------------------------------------------------------------- GPU arm --
+def gpu_arm(args, rank, world, local):
+    import ctypes as C
+
+    import torch
+
+    import nbgb
+    from nbgb.serving import Ensemble, serve
+
+    torch.cuda.set_device(local)
+    dev_index = torch.cuda.current_device()
+    lib = nbgb.lib()
+    ffma, ffma2, mufu = C.c_double(), C.c_double(), C.c_double()
+    nbgb.check(lib.nbgb_measure_fp32_peak(C.byref(ffma), C.byref(ffma2), C.byref(mufu)))
+
+    stream_seed = 5 + 1000 * rank
+    stream = nbgb.ics.ensemble_requests(4096, seed=stream_seed)
+    S = args.resident
+    # --- batched, saturation --------------------------------------------------
+    backlog = stream[: S + 256]
+    states = {r["id"]: make_state(nbgb, r) for r in backlog}
+    ens = Ensemble(hbm_budget_bytes=64 << 30, max_resident=S, softening=EPS, theta=0.5)
+    for r in backlog:
+        ens.submit(states[r["id"]], r["steps"], DT)
+    prime = 0
+    while True:  # admission + autotuning outside the measurement
+        ens.tick()
+        prime += 1
+        if (ens.stats()["tuning"] == 0 and prime >= 3) or prime >= 60:
+            break
+    for _ in range(args.warmup):
+        ens.tick()
+    est = torch.cuda.ExternalStream(ens.stream())
+    s0 = ens.stats()
+    resident_bytes = s0["bytes_reserved"]
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(dev_index) as clk:
+        e0.record(est)
+        t_host = time.perf_counter()
+        for _ in range(args.steps):
+            ens.tick()
+        e1.record(est)
+        torch.cuda.synchronize()
+        host_s = time.perf_counter() - t_host
+    elapsed_s = e0.elapsed_time(e1) / 1e3
+    s1 = ens.stats()
+    ps = s1["particle_steps"] - s0["particle_steps"]
+    dint = s1["direct_kernel_interactions"] - s0["direct_kernel_interactions"]
+    dms = s1["direct_kernel_ms"] - s0["direct_kernel_ms"]
+    bh_int = s1["bh_interactions"] - s0["bh_interactions"]
+    launches = s1["kernel_launches"] - s0["kernel_launches"]
+    tuned = s1["direct_config"]
+    ens.close()
+    del states
+
+    # --- reduction over ranks ---------------------------------------------------
+    t_max = elapsed_s
+    ps_tot = ps
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([elapsed_s], dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+        pt = torch.tensor([float(ps)], dtype=torch.float64)
+        dist.all_reduce(pt, op=dist.ReduceOp.SUM)
+        ps_tot = float(pt.item())
+    value = ps_tot / t_max
+
+    out = {}
+    if rank == 0:
+        # --- plain: one request at a time --------------------------------------
+        plain = None
+        if not args.no_plain:
+            plain = plain_arm(nbgb, stream[: args.plain_requests], args.plain_steps)
+        # --- serving: Poisson arrivals at 80 % load, latency, e2e ---------------
+        serve_rep = None
+        if not args.no_serve:
+            sreqs = nbgb.ics.ensemble_requests(args.serve_requests, seed=stream_seed + 7)
+            work = request_work(sreqs) / len(sreqs)  # particle-steps per request
+            rate = 0.8 * value / work  # requests per second at 80 % of capacity
+            for r in sreqs:
+                r["arrival"] = r["arrival"] / rate  # unit-rate stream -> target rate
+            cache = {}
+
+            def mk(req):
+                st = cache.pop(req["id"], None)
+                return st if st is not None else make_state(nbgb, req)
+
+            for r in sreqs[:64]:
+                cache[r["id"]] = make_state(nbgb, r)
+            ens2 = Ensemble(hbm_budget_bytes=64 << 30, softening=EPS, theta=0.5)
+            rep = serve(ens2, sreqs, mk, dt=DT, time_scale=1.0, max_wall_s=args.serve_max_s)
+            ens2.close()
+            h2d = sum(7 * 4 * r["n"] for r in sreqs)
+            d2h = sum((6 * 8 + 4 * 4) * r["n"] for r in sreqs)
+            serve_rep = dict(rate_req_s=rate, completed=rep.completed, offered=len(sreqs),
+                             wall_s=rep.wall_s, particle_steps=rep.particle_steps,
+                             ticks=rep.ticks, p50_s=rep.percentile(50), p99_s=rep.percentile(99),
+                             h2d=h2d, d2h=d2h)
+        # --- CPU baseline (reference CPU path, restated) -------------------------
+        cpu = cpu_baseline(nbgb, stream, args.cpu_seconds)
+
+        ffma_peak = ffma.value
+        achieved = 20.0 * dint / (dms / 1e3) / 1e12 if dms > 0 else None
+        direct_share = (dms / 1e3) / elapsed_s if elapsed_s > 0 else None
+        clocks = clk.summary()
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Plummer clusters; no dataset)",
+            "config": {
+                "workload": WORKLOAD, "resident_systems": S, "backlog_requests": len(backlog),
+                "tick": "one Velocity-Verlet step of every resident system",
+                "l2": f"not flushed; resident state + trees {resident_bytes / 2**20:.0f} MiB > "
+                      f"L2 {L2_BYTES / 2**20:.0f} MiB",
+                "direct_kernel_config": tuned, "theta": 0.5, "softening": EPS, "dt": DT,
+                "force_error": "direct: compensated FP32, median rel err ~1e-7 vs FP64; "
+                               "Barnes-Hut theta=0.5: median rel err <= 2e-3 vs FP64 "
+                               "(tests/test_bh_gpu.py, tests/test_direct_gpu.py)",
+                "parallelism": f"replicas x{world} (request-stream shards)",
+            },
+            "batched_particle_steps_per_s": value,
+            "plain_particle_steps_per_s": plain["value"] if plain else None,
+            "batched_vs_plain": (value / world / plain["value"]) if plain else None,
+            "plain": plain,
+            "interactions_per_s": (dint + bh_int) / t_max,
+            "direct_interactions_per_s": dint / t_max,
+            "bh_interactions_per_s": bh_int / t_max,
+            "host_s": host_s,
+            "latency_p50_s": serve_rep["p50_s"] if serve_rep else None,
+            "latency_p99_s": serve_rep["p99_s"] if serve_rep else None,
+            "serve": serve_rep,
+            "e2e": ({"value": serve_rep["particle_steps"] / serve_rep["wall_s"], "unit": UNIT,
+                     "h2d_bytes_per_step": serve_rep["h2d"] / max(serve_rep["ticks"], 1),
+                     "d2h_bytes_per_step": serve_rep["d2h"] / max(serve_rep["ticks"], 1),
+                     "note": "Poisson serving run at 80% of capacity through the public "
+                             "API: host arrays submitted, results polled to the host"}
+                    if serve_rep else None),
+            "roofline": {
+                "kernel": "ens_direct_kernel (direct-sum work queue)",
+                "bound": "fp32", "achieved": achieved, "peak": ffma_peak, "unit": "TFLOP/s",
+                "frac": (achieved / ffma_peak) if achieved else None,
+                "traffic": None,
+                "peak_source": "measured in-process: FFMA chains on every SM "
+                               "(nbgb_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
+                "flops_per_interaction": 20, "share_of_tick": direct_share,
+                "hbm_peak_gbs_measured": measured_peaks().get("hbm_gbs"),
+            },
+            "fp32_peaks": {"ffma_tflops": ffma.value, "ffma2_tflops": ffma2.value,
+                           "mufu_gops": mufu.value},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "gpu_launches": launches,
+        }
+    return out
+
+
+def plain_arm(nbgb, reqs, steps) -> dict:
+    """Each request alone through the plain device path, in sequence."""
+    tot_ps, tot_s = 0.0, 0.0
+    per = []
+    for r in reqs:
+        s = make_state(nbgb, r)
+        if r["n"] <= 8192:
+            calc = nbgb.DirectForceCalculator()
+        else:
+            calc = nbgb.BarnesHutCalculator(0.5)
+        calc.setSofteningParameter(EPS)
+        sysm = nbgb.System(calc, s)
+        sysm.step(DT, 2)  # warm
+        t0 = time.perf_counter()
+        sysm.step(DT, steps)  # synchronizes at the end
+        dt = time.perf_counter() - t0
+        sysm.close()
+        calc.close()
+        tot_ps += r["n"] * steps
+        tot_s += dt
+        per.append((r["n"], dt / steps))
+    return {"value": tot_ps / tot_s, "requests": len(reqs), "steps_each": steps,
+            "ms_per_step_by_n": [[n, 1e3 * t] for n, t in per[:12]]}
+
+
+def cpu_baseline(nbgb, stream, seconds) -> dict:
+    """The reference's CPU path (pair-function direct sum in reference order,
+    Velocity-Verlet formulae; the reference insertion octree + walk for the
+    Barnes-Hut systems) restated in oracle/, one step per sampled system."""
+    from oracle.oracle import Oracle
+    orc = Oracle()
+    ps, t = 0.0, 0.0
+    count = 0
+    for r in stream:
+        if t > seconds:
+            break
+        s = make_state(nbgb, r)
+        x, y, z, m = s["x"].copy(), s["y"].copy(), s["z"].copy(), s["m"]
+        vx, vy, vz = s["vx"].copy(), s["vy"].copy(), s["vz"].copy()
+        if r["n"] <= 8192:
+            ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)  # a(t) of a running system
+            t0 = time.perf_counter()
+            ox, oy, oz = ax.copy(), ay.copy(), az.copy()
+            orc.update_positions(x, y, z, vx, vy, vz, ax, ay, az, DT)
+            ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
+            orc.update_velocities(vx, vy, vz, ox, oy, oz, ax, ay, az, DT)
+            steps = 1
+            dt = time.perf_counter() - t0
+        else:
+            t0 = time.perf_counter()
+            bmin, bmax = orc.bbox(x, y, z)
+            _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
+            nodes, _, _ = orc.build_octree(x, y, z, m, si, bmin, bmax)
+            orc.bh_forces(nodes, x, y, z, m, 0.5, 1.0, EPS)
+            steps = 1
+            dt = time.perf_counter() - t0
+        ps += r["n"] * steps
+        t += dt
+        count += 1
+    return {"value": ps / t if t > 0 else None, "unit": UNIT, "cores": orc.num_threads(),
+            "kind": "port",
+            "sample": f"{count} systems of the same request stream, one Velocity-Verlet step "
+                      f"each on the host (direct: reference pair function order; N>8192: "
+                      f"reference insertion octree + walk), {t:.1f} s of CPU time"}
+
+
+# ----------------------------------------------------------- reference arm --
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return None
+    import nbgb  # only for the request stream and the initial conditions
+    stream = nbgb.ics.ensemble_requests(4096, seed=5)
+    from oracle.oracle import Oracle
+    orc = Oracle()
+    per_step = max(2.0, 120.0 / max(args.steps + args.warmup, 1))
+    results = []
+    idx = 0
+    for k in range(args.warmup + args.steps):
+        ps, t = 0.0, 0.0
+        while t < per_step and idx < len(stream):
+            r = stream[idx]
+            idx += 1
+            if r["n"] > 8192:
+                continue  # a bounded sample of the direct part keeps each step short
+            s = make_state(nbgb, r)
+            x, y, z, m = s["x"].copy(), s["y"].copy(), s["z"].copy(), s["m"]
+            vx, vy, vz = s["vx"].copy(), s["vy"].copy(), s["vz"].copy()
+            ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
+            t0 = time.perf_counter()
+            ox, oy, oz = ax.copy(), ay.copy(), az.copy()
+            orc.update_positions(x, y, z, vx, vy, vz, ax, ay, az, DT)
+            ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
+            orc.update_velocities(vx, vy, vz, ox, oy, oz, ax, ay, az, DT)
+            t += time.perf_counter() - t0
+            ps += r["n"]
+        if k >= args.warmup:
+            results.append((ps, t))
+    tot_ps = sum(p for p, _ in results)
+    tot_t = sum(t for _, t in results)
+    value = tot_ps / tot_t if tot_t > 0 else 0.0
+    sample = (f"per step: direct-method systems (N<=8192) of the request stream, one "
+              f"Velocity-Verlet step each, ~{per_step:.0f} s of CPU work; reference pair "
+              f"function in reference order")
+    return {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot_t / max(len(results), 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded Plummer clusters; no dataset)",
+        "config": {"workload": WORKLOAD, "path": "reference host CPU path (restated)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": orc.num_threads(),
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> int:
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        out = reference_arm(args, rank, world)
+    else:
+        out = gpu_arm(args, rank, world, local)
+    if rank == 0 and out:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -228,6 +228,90 @@ nbgb_status nbgb_system_read_f64(nbgb_system* sys, double* x, double* y, double*
 nbgb_status nbgb_system_energy(nbgb_system* sys, double* ke, double* pe, double momentum[3]);
 
 /* ---------------------------------------------------------------------------
+ * Ensemble serving (no reference counterpart; the reference runs one
+ * ParticleSystem at a time).  Many independent simulations share the GPU:
+ * requests are admitted while the HBM budget and the resident cap allow,
+ * every resident system advances one Velocity-Verlet step per tick (FP64
+ * x/v state, FP32 forces: direct sum for N <= direct_max_n through one
+ * persistent work-queue kernel spanning all direct systems, Barnes-Hut per
+ * system as a CUDA graph on a stream pool), and finished systems retire and
+ * free their memory.  The result of a system does not depend on what else
+ * is resident (per-system work decomposition), except through the direct
+ * kernel configuration the autotuner picks (rounding-level differences).
+ * ------------------------------------------------------------------------- */
+typedef struct nbgb_ensemble nbgb_ensemble;
+
+typedef struct nbgb_ensemble_config {
+  uint64_t hbm_budget_bytes; /* admission budget for system state and trees */
+  int32_t max_resident;      /* cap on simultaneously resident systems */
+  int32_t direct_max_n;      /* N <= direct_max_n: direct sum, else Barnes-Hut */
+  float G;
+  float softening;           /* must be > 0 */
+  float theta;               /* Barnes-Hut opening angle */
+  int32_t leaf_capacity;     /* Barnes-Hut bucket size (1 = reference tree walk) */
+  int32_t direct_config;     /* direct kernel configuration; -1 = autotune */
+  int32_t use_graphs;        /* capture each Barnes-Hut step as a CUDA graph */
+} nbgb_ensemble_config;
+
+/* One finished request. */
+typedef struct nbgb_ensemble_result {
+  uint64_t request_id;
+  int64_t count;
+  int32_t steps;
+  int32_t method;        /* nbgb_method used */
+  double gpu_ms;         /* tick time from admission to retirement */
+} nbgb_ensemble_result;
+
+typedef struct nbgb_ensemble_stats {
+  int64_t ticks;
+  int64_t particle_steps;       /* sum over ticks of resident bodies */
+  double direct_interactions;   /* sum of N (N - 1) over direct system-steps */
+  double bh_interactions;       /* accepted interactions (measured at admission) x steps */
+  int64_t admitted;
+  int64_t retired;
+  int32_t resident;
+  int32_t queued;
+  uint64_t bytes_reserved;      /* against hbm_budget_bytes */
+  int32_t direct_config;        /* configuration in use */
+  int32_t tuning;               /* 1 while the autotuner is measuring */
+  double direct_kernel_ms;      /* summed device time of the direct work-queue kernel */
+  double direct_kernel_interactions; /* interactions those launches computed */
+  int64_t kernel_launches;      /* kernels launched by ticks (graph kernel nodes counted) */
+} nbgb_ensemble_stats;
+
+void nbgb_ensemble_config_default(nbgb_ensemble_config* cfg);
+nbgb_status nbgb_ensemble_create(const nbgb_ensemble_config* cfg, nbgb_ensemble** out);
+nbgb_status nbgb_ensemble_destroy(nbgb_ensemble* ens);
+/* Queue a simulation: HOST pos/vel/mass arrays of h_init, `steps` steps of
+ * size dt.  The arrays are copied; the call does not touch the GPU. */
+nbgb_status nbgb_ensemble_submit(nbgb_ensemble* ens, const nbgb_particle_data* h_init,
+                                 int32_t steps, float dt, uint64_t* request_id);
+/* Admit what fits, advance every resident system one step, retire the
+ * finished ones (their results become pollable when their copies land). */
+nbgb_status nbgb_ensemble_tick(nbgb_ensemble* ens, int32_t* resident, int32_t* queued);
+/* Pop one finished request.  Returns NBGB_ERR_NOT_READY when none is
+ * available.  If h_out is non-NULL its pos/vel/acc/mass arrays (count
+ * entries, host) receive the final FP32 state; state_f64 (6*count doubles
+ * x, y, z, vx, vy, vz, or NULL) the FP64 state. */
+nbgb_status nbgb_ensemble_poll(nbgb_ensemble* ens, nbgb_ensemble_result* result,
+                               nbgb_particle_data* h_out, double* state_f64);
+/* Wait for all retirements in flight. */
+nbgb_status nbgb_ensemble_synchronize(nbgb_ensemble* ens);
+nbgb_status nbgb_ensemble_get_stats(nbgb_ensemble* ens, nbgb_ensemble_stats* stats);
+/* The stream every tick's work joins into (for CUDA-event timing). */
+nbgb_status nbgb_ensemble_get_stream(nbgb_ensemble* ens, void** cuda_stream);
+
+/* ---------------------------------------------------------------------------
+ * FP64 direct sum on the GPU (the full-FP64 variant of the precision study;
+ * no reference counterpart).  Sources: n_src device float4 (x, y, z, m);
+ * targets: device indices into the sources (or NULL for all); device double
+ * outputs.  Same law as nbgb_compute_forces, self term excluded.
+ * ------------------------------------------------------------------------- */
+nbgb_status nbgb_direct_f64(const float* d_src_xyzm, int64_t n_src, const int64_t* d_targets,
+                            int64_t n_targets, double G, double eps, double* d_ax, double* d_ay,
+                            double* d_az, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Diagnostics (no reference counterpart): measured FP32 pipe rates of the
  * current device -- FFMA and packed FFMA2 in TFLOP/s (2 flops per lane-FMA)
  * and MUFU rsqrt in Gop/s -- used as roofline denominators for the force

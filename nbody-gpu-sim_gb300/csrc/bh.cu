@@ -573,12 +573,31 @@ static void bh_build(nbgb_calculator* c, BHState& h, const float4* pm, int64_t n
   NBGB_LAUNCH_CHECK();
 }
 
+size_t bh_state_bytes(const BHState* p) {
+  if (!p) return 0;
+  const BHState& h = *p;
+  return h.bbox_part.bytes() + h.box.bytes() + h.mkeys.bytes() + h.mkeys_alt.bytes() +
+         h.midx.bytes() + h.midx_alt.bytes() + h.klo.bytes() + h.klo_alt.bytes() +
+         h.khi.bytes() + h.khi_alt.bytes() + h.pidx.bytes() + h.pidx_alt.bytes() +
+         h.hist.bytes() + h.scan_ws.bytes() + h.lcp.bytes() + h.ncnt.bytes() + h.nstart.bytes() +
+         h.scalars.bytes() + h.node_com.bytes() + h.node_geom.bytes() + h.node_info.bytes() +
+         h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() + h.spm.bytes();
+}
+
+// Node capacity that any realistic input fits (the canonical tree has ~1.5N
+// nodes; 4N + 64 leaves room for strongly clustered sets).  Used when the
+// calculator runs without per-call synchronization (no read-back to regrow).
+static int64_t bh_async_capacity(int64_t n) { return 4 * n + 64; }
+
 void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float* ay, float* az) {
   if (!c->bh) c->bh.reset(new BHState());
   BHState& h = *c->bh;
   cudaStream_t st = c->stream;
+  const bool sync = (c->params.flags & NBGB_FLAG_SYNC) != 0;
+  if (!sync && h.cap < bh_async_capacity(n)) h.cap = bh_async_capacity(n);
   for (int attempt = 0; attempt < 2; ++attempt) {
     bh_build(c, h, pm, n);
+    if (!sync) break;  // capacity overflow surfaces through the device error word
     // The node count is data dependent: read it back and regrow once if the
     // capacity was too small (the kernels skipped their work in that case).
     uint32_t* hs = h.h_scalars.ensure(2);

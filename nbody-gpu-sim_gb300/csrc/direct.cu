@@ -16,6 +16,7 @@
 // per j-tile).  COMP = false gives the plain single-accumulator FP32 sum.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "direct_core.cuh"
 
 namespace nbgb {
 
@@ -41,13 +42,16 @@ void launch_pack_soa(const float* x, const float* y, const float* z, const float
 }
 
 // ---------------------------------------------------------------------------
-// The direct kernel.
+// The direct kernel: CTA (blockIdx.x) owns kDirThreads*I targets, split
+// (blockIdx.y) owns a contiguous run of j-tiles.
 // ---------------------------------------------------------------------------
 template <int I, bool PAIRED, bool COMP, bool ZERO_SOFT>
 __global__ void __launch_bounds__(kDirThreads) direct_kernel(DirectArgs a) {
   static_assert(!PAIRED || (I % 2 == 0), "paired path needs an even target count");
   __shared__ alignas(128) float4 s_j[kDirStages][kDirTile];
   __shared__ alignas(8) uint64_t s_bar[kDirStages];
+  TileRing ring{s_j, s_bar, 0};
+  ring_init(ring);
 
   const int tid = threadIdx.x;
   const int64_t tgt_base = (int64_t)blockIdx.x * (kDirThreads * I);
@@ -55,19 +59,6 @@ __global__ void __launch_bounds__(kDirThreads) direct_kernel(DirectArgs a) {
   const int64_t tile0 = (int64_t)split * a.tiles_per_split;
   const int64_t tile1 = imin64(tile0 + a.tiles_per_split, a.n_tiles);
   const int nt = (int)imax64(tile1 - tile0, 0);
-  constexpr uint32_t kBytes = kDirTile * sizeof(float4);
-
-  if (tid == 0) {
-    for (int s = 0; s < kDirStages; ++s) mbar_init(&s_bar[s], 1);
-    fence_barrier_init();
-  }
-  __syncthreads();
-  if (tid == 0) {
-    for (int s = 0; s < kDirStages && s < nt; ++s) {
-      mbar_arrive_expect_tx(&s_bar[s], kBytes);
-      bulk_g2s(s_j[s], a.src + (tile0 + s) * kDirTile, kBytes, &s_bar[s]);
-    }
-  }
 
   // Targets: thread tid owns tgt_base + tid + q*kDirThreads (coalesced I/O).
   float xi[I], yi[I], zi[I];
@@ -79,135 +70,22 @@ __global__ void __launch_bounds__(kDirThreads) direct_kernel(DirectArgs a) {
     yi[q] = p.y;
     zi[q] = p.z;
   }
-  float sx[I], sy[I], sz[I], ex[I], ey[I], ez[I];
-#pragma unroll
-  for (int q = 0; q < I; ++q) sx[q] = sy[q] = sz[q] = ex[q] = ey[q] = ez[q] = 0.f;
-
-  const float eps2 = a.eps2;
-  bool bad = false;
-  for (int t = 0; t < nt; ++t) {
-    const int s = t % kDirStages;
-    const uint32_t parity = (uint32_t)(t / kDirStages) & 1u;
-    if (!bad && !mbar_wait(&s_bar[s], parity, a.err)) bad = true;
-    if (!bad) {
-      const float4* __restrict__ tile = s_j[s];
-      float tx[I], ty[I], tz[I];
-#pragma unroll
-      for (int q = 0; q < I; ++q) tx[q] = ty[q] = tz[q] = 0.f;
-      if constexpr (PAIRED) {
-        constexpr int P = I / 2;
-        f2 xp[P], yp[P], zp[P], ax2[P], ay2[P], az2[P];
-#pragma unroll
-        for (int p = 0; p < P; ++p) {
-          xp[p] = f2_make(xi[2 * p], xi[2 * p + 1]);
-          yp[p] = f2_make(yi[2 * p], yi[2 * p + 1]);
-          zp[p] = f2_make(zi[2 * p], zi[2 * p + 1]);
-          ax2[p] = ay2[p] = az2[p] = f2_make(0.f, 0.f);
-        }
-        const f2 e2 = f2_make(eps2, eps2);
-#pragma unroll 4
-        for (int k = 0; k < kDirTile; ++k) {
-          const float4 pj = tile[k];
-          const f2 xj = f2_make(pj.x, pj.x), yj = f2_make(pj.y, pj.y), zj = f2_make(pj.z, pj.z);
-          const f2 mj = f2_make(pj.w, pj.w);
-#pragma unroll
-          for (int p = 0; p < P; ++p) {
-            f2 dx = f2_sub(xj, xp[p]);
-            f2 dy = f2_sub(yj, yp[p]);
-            f2 dz = f2_sub(zj, zp[p]);
-            f2 d2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, e2)));
-            float d2l, d2h;
-            f2_split(d2, d2l, d2h);
-            float rl = rsqrt_approx(d2l), rh = rsqrt_approx(d2h);
-            if constexpr (ZERO_SOFT) {
-              rl = (d2l > 0.f) ? rl : 0.f;
-              rh = (d2h > 0.f) ? rh : 0.f;
-            }
-            f2 r = f2_make(rl, rh);
-            f2 f = f2_mul(f2_mul(mj, r), f2_mul(r, r));
-            ax2[p] = f2_fma(f, dx, ax2[p]);
-            ay2[p] = f2_fma(f, dy, ay2[p]);
-            az2[p] = f2_fma(f, dz, az2[p]);
-          }
-        }
-#pragma unroll
-        for (int p = 0; p < P; ++p) {
-          f2_split(ax2[p], tx[2 * p], tx[2 * p + 1]);
-          f2_split(ay2[p], ty[2 * p], ty[2 * p + 1]);
-          f2_split(az2[p], tz[2 * p], tz[2 * p + 1]);
-        }
-      } else {
-#pragma unroll 4
-        for (int k = 0; k < kDirTile; ++k) {
-          const float4 pj = tile[k];
-#pragma unroll
-          for (int q = 0; q < I; ++q) {
-            float dx = pj.x - xi[q];
-            float dy = pj.y - yi[q];
-            float dz = pj.z - zi[q];
-            float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-            float r = rsqrt_approx(d2);
-            if constexpr (ZERO_SOFT) r = (d2 > 0.f) ? r : 0.f;
-            float f = (pj.w * r) * (r * r);
-            tx[q] = fmaf(f, dx, tx[q]);
-            ty[q] = fmaf(f, dy, ty[q]);
-            tz[q] = fmaf(f, dz, tz[q]);
-          }
-        }
-      }
-#pragma unroll
-      for (int q = 0; q < I; ++q) {
-        if constexpr (COMP) {
-          float e;
-          sx[q] = two_sum(sx[q], tx[q], e);
-          ex[q] += e;
-          sy[q] = two_sum(sy[q], ty[q], e);
-          ey[q] += e;
-          sz[q] = two_sum(sz[q], tz[q], e);
-          ez[q] += e;
-        } else {
-          sx[q] += tx[q];
-          sy[q] += ty[q];
-          sz[q] += tz[q];
-        }
-      }
-    }
-    if (__syncthreads_or(bad)) {
-      bad = true;
-      break;
-    }
-    if (tid == 0 && t + kDirStages < nt) {
-      fence_proxy_async_smem();
-      mbar_arrive_expect_tx(&s_bar[s], kBytes);
-      bulk_g2s(s_j[s], a.src + (tile0 + t + kDirStages) * kDirTile, kBytes, &s_bar[s]);
-    }
-  }
-  if (bad) {
-    // Drain (bounded) any copy still in flight before the CTA's shared
-    // memory is released.
-    if (tid == 0) {
-      for (int s = 0; s < kDirStages && s < nt; ++s) {
-        int last = ((nt - 1 - s) / kDirStages) * kDirStages + s;  // last tile issued on stage s
-        mbar_wait(&s_bar[s], (uint32_t)(last / kDirStages) & 1u, nullptr, 1u << 16);
-      }
-    }
+  float sx[I], sy[I], sz[I];
+  if (!direct_tiles<kDirThreads, I, PAIRED, COMP, ZERO_SOFT>(ring, a.src + tile0 * kDirTile, nt,
+                                                             xi, yi, zi, a.eps2, sx, sy, sz,
+                                                             a.err))
     return;
-  }
-
   const float G = a.G;
 #pragma unroll
   for (int q = 0; q < I; ++q) {
     int64_t i = tgt_base + tid + (int64_t)q * kDirThreads;
     if (i >= a.n_tgt) continue;
-    float rx = COMP ? sx[q] + ex[q] : sx[q];
-    float ry = COMP ? sy[q] + ey[q] : sy[q];
-    float rz = COMP ? sz[q] + ez[q] : sz[q];
     if (a.partial) {
-      a.partial[(int64_t)split * a.n_tgt_pad + i] = make_float4(rx, ry, rz, 0.f);
+      a.partial[(int64_t)split * a.n_tgt_pad + i] = make_float4(sx[q], sy[q], sz[q], 0.f);
     } else {
-      a.out_x[i] = G * rx;
-      a.out_y[i] = G * ry;
-      a.out_z[i] = G * rz;
+      a.out_x[i] = G * sx[q];
+      a.out_y[i] = G * sy[q];
+      a.out_z[i] = G * sz[q];
     }
   }
 }
@@ -475,3 +353,70 @@ void launch_potential(const float4* src, int64_t n, float eps2, double* partials
 }
 
 }  // namespace nbgb
+
+// ---------------------------------------------------------------------------
+// FP64 direct sum (the full-FP64 variant; accuracy reference on the GPU).
+// ---------------------------------------------------------------------------
+namespace nbgb {
+
+__global__ void direct_f64_kernel(const float4* __restrict__ src, int64_t n_src,
+                                  const int64_t* __restrict__ targets, int64_t n_tgt, double G,
+                                  double eps2, double* __restrict__ ax, double* __restrict__ ay,
+                                  double* __restrict__ az) {
+  __shared__ float4 s_j[256];
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_tgt;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = base + threadIdx.x;
+    const bool valid = t < n_tgt;
+    const int64_t i = valid ? (targets ? targets[t] : t) : 0;
+    const float4 pi = src[i];
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int64_t c = 0; c < n_src; c += 256) {
+      __syncthreads();
+      const int64_t j = c + threadIdx.x;
+      s_j[threadIdx.x] = (j < n_src) ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+      __syncthreads();
+      const int lim = (int)imin64(256, n_src - c);
+      for (int k = 0; k < lim; ++k) {
+        if (c + k == i) continue;
+        const float4 pj = s_j[k];
+        const double dx = (double)pj.x - (double)pi.x, dy = (double)pj.y - (double)pi.y,
+                     dz = (double)pj.z - (double)pi.z;
+        const double d2 = dx * dx + dy * dy + dz * dz + eps2;
+        const double inv = 1.0 / sqrt(d2);
+        const double f = (double)pj.w * inv * inv * inv;
+        sx += f * dx;
+        sy += f * dy;
+        sz += f * dz;
+      }
+    }
+    if (valid) {
+      ax[t] = G * sx;
+      ay[t] = G * sy;
+      az[t] = G * sz;
+    }
+  }
+}
+
+}  // namespace nbgb
+
+extern "C" nbgb_status nbgb_direct_f64(const float* d_src_xyzm, int64_t n_src,
+                                       const int64_t* d_targets, int64_t n_targets, double G,
+                                       double eps, double* d_ax, double* d_ay, double* d_az,
+                                       void* stream) {
+  using namespace nbgb;
+  try {
+    if (!d_src_xyzm || !d_ax || !d_ay || !d_az || n_src < 0 || n_targets < 0)
+      return NBGB_ERR_INVALID_ARG;
+    if (n_targets == 0) return NBGB_OK;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t blocks = std::min<int64_t>(ceil_div(n_targets, 256), (int64_t)num_sms() * 8);
+    direct_f64_kernel<<<(unsigned)blocks, 256, 0, st>>>(
+        reinterpret_cast<const float4*>(d_src_xyzm), n_src, d_targets, n_targets, G, eps * eps,
+        d_ax, d_ay, d_az);
+    NBGB_LAUNCH_CHECK();
+    return NBGB_OK;
+  } catch (const Error& e) {
+    return e.status;
+  }
+}

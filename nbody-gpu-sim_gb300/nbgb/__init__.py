@@ -7,7 +7,7 @@ include/nbgb.h).  This package is its host-side mirror of the reference's
 """
 from .api import *  # noqa: F401,F403
 from .api import __all__ as _api_all
-from . import ics, checkpoint  # noqa: F401
+from . import ics, checkpoint, serving  # noqa: F401
 from ._lib import lib, lib_path, declared_symbols  # noqa: F401
 
 __all__ = list(_api_all) + ["ics", "checkpoint", "lib", "lib_path", "declared_symbols"]

@@ -34,6 +34,28 @@ class OctreeNode(C.Structure):
                 ("is_leaf", C.c_uint8), ("pad_", C.c_uint8 * 3), ("particle_count", C.c_int32)]
 
 
+class EnsembleConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_resident", C.c_int32),
+                ("direct_max_n", C.c_int32), ("G", C.c_float), ("softening", C.c_float),
+                ("theta", C.c_float), ("leaf_capacity", C.c_int32), ("direct_config", C.c_int32),
+                ("use_graphs", C.c_int32)]
+
+
+class EnsembleResult(C.Structure):
+    _fields_ = [("request_id", C.c_uint64), ("count", C.c_int64), ("steps", C.c_int32),
+                ("method", C.c_int32), ("gpu_ms", C.c_double)]
+
+
+class EnsembleStats(C.Structure):
+    _fields_ = [("ticks", C.c_int64), ("particle_steps", C.c_int64),
+                ("direct_interactions", C.c_double), ("bh_interactions", C.c_double),
+                ("admitted", C.c_int64), ("retired", C.c_int64), ("resident", C.c_int32),
+                ("queued", C.c_int32), ("bytes_reserved", C.c_uint64),
+                ("direct_config", C.c_int32), ("tuning", C.c_int32),
+                ("direct_kernel_ms", C.c_double), ("direct_kernel_interactions", C.c_double),
+                ("kernel_launches", C.c_int64)]
+
+
 assert C.sizeof(OctreeNode) == 76
 assert C.sizeof(ParticleDataStruct) == 13 * 8 + 8
 
@@ -82,6 +104,17 @@ _SIGS = {
     "nbgb_system_read_f64": (C.c_int, [_vp] + [_vp] * 6),
     "nbgb_system_energy": (C.c_int, [_vp, _f64p, _f64p, _f64p]),
     "nbgb_measure_fp32_peak": (C.c_int, [_f64p, _f64p, _f64p]),
+    "nbgb_direct_f64": (C.c_int, [_vp, C.c_int64, _vp, C.c_int64, C.c_double, C.c_double,
+                                  _vp, _vp, _vp, _vp]),
+    "nbgb_ensemble_config_default": (None, [C.POINTER(EnsembleConfig)]),
+    "nbgb_ensemble_create": (C.c_int, [C.POINTER(EnsembleConfig), C.POINTER(_vp)]),
+    "nbgb_ensemble_destroy": (C.c_int, [_vp]),
+    "nbgb_ensemble_submit": (C.c_int, [_vp, _pd, C.c_int32, C.c_float, C.POINTER(C.c_uint64)]),
+    "nbgb_ensemble_tick": (C.c_int, [_vp, _i32p, _i32p]),
+    "nbgb_ensemble_poll": (C.c_int, [_vp, C.POINTER(EnsembleResult), _pd, _vp]),
+    "nbgb_ensemble_synchronize": (C.c_int, [_vp]),
+    "nbgb_ensemble_get_stats": (C.c_int, [_vp, C.POINTER(EnsembleStats)]),
+    "nbgb_ensemble_get_stream": (C.c_int, [_vp, C.POINTER(_vp)]),
     "nbgb_last_error": (C.c_char_p, []),
     "nbgb_version": (C.c_char_p, []),
     "nbgb_abi_version": (C.c_int32, []),

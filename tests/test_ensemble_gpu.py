@@ -1,0 +1,153 @@
+"""Ensemble serving through the C ABI (GPU).
+
+* Each result is the same alone and in the mix: with a fixed direct-kernel
+  configuration the final FP64 state of a system is bitwise identical
+  whether it ran alone or among other systems (direct and Barnes-Hut), since
+  its work decomposition does not depend on the mix.  With the autotuner on,
+  the same holds within 1e-9 relative (only the direct kernel configuration
+  may differ, changing summation order).
+* Against the plain one-system path (nbgb_system) and the FP64 oracle: final
+  positions within 2e-5, velocities within 2e-4 (100 steps, dt = 1e-3).
+* Admission respects the HBM budget and the resident cap; everything
+  submitted completes; memory is returned.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(nb, reqs, **cfg):
+    from nbgb.serving import Ensemble
+    ens = Ensemble(**cfg)
+    ids = {}
+    for key, (state, steps) in reqs.items():
+        ids[ens.submit(state, steps, 1e-3)] = key
+    out = {}
+    guard = 0
+    while len(out) < len(reqs):
+        ens.tick()
+        while True:
+            got = ens.poll(want_state=True)
+            if got is None:
+                break
+            res, st = got
+            out[ids[res["request_id"]]] = (res, st)
+        guard += 1
+        assert guard < 10000
+    stats = ens.stats()
+    ens.close()
+    return out, stats
+
+
+def _systems(nb):
+    return {
+        "d300": (nb.ics.plummer(300, seed=11), 40),
+        "d2000": (nb.ics.plummer(2000, seed=12), 25),
+        "d5000": (nb.ics.plummer(5000, seed=13), 30),
+        "b9000": (nb.ics.plummer(9000, seed=14), 20),
+        "b20000": (nb.ics.plummer(20000, seed=15), 15),
+    }
+
+
+def test_same_alone_and_in_mix_bitwise(nb):
+    sy = _systems(nb)
+    mixed, _ = _run(nb, sy, direct_config=0, hbm_budget_bytes=4 << 30)
+    for key in ("d2000", "b9000"):
+        alone, _ = _run(nb, {key: sy[key]}, direct_config=0, hbm_budget_bytes=4 << 30)
+        for k in ("x", "y", "z", "vx", "vy", "vz"):
+            np.testing.assert_array_equal(alone[key][1][k], mixed[key][1][k])
+
+
+def test_same_alone_and_in_mix_autotuned(nb):
+    sy = _systems(nb)
+    mixed, stats = _run(nb, sy, hbm_budget_bytes=4 << 30)
+    alone, _ = _run(nb, {"d5000": sy["d5000"]}, hbm_budget_bytes=4 << 30)
+    for k in ("x", "y", "z"):
+        a, b = alone["d5000"][1][k], mixed["d5000"][1][k]
+        assert np.max(np.abs(a - b)) <= 1e-9 * max(1.0, np.max(np.abs(a)))
+    assert stats["retired"] == len(sy)
+
+
+def test_matches_plain_system_and_fp64_oracle(nb, orc):
+    s = nb.ics.plummer(1500, seed=21)
+    steps = 100
+    res, _ = _run(nb, {"a": (s, steps)}, direct_config=1)
+    got = res["a"][1]
+    calc = nb.DirectForceCalculator()
+    calc.setSofteningParameter(0.01)
+    sysm = nb.System(calc, s)
+    sysm.step(1e-3, steps)
+    plain = sysm.read_f64()
+    sysm.close()
+    calc.close()
+    st = {k: s[k].astype(np.float64) for k in ("x", "y", "z", "vx", "vy", "vz")}
+    m = s["m"].astype(np.float64)
+    st["ax"], st["ay"], st["az"] = orc.direct_f64(st["x"], st["y"], st["z"], m, 1.0, 0.01)
+    for _ in range(steps):
+        orc.vv_step_f64(st, m, 1.0, 0.01, 1e-3)
+    for ref in (plain, st):
+        assert max(np.abs(got[k] - ref[k]).max() for k in ("x", "y", "z")) <= 2e-5
+        assert max(np.abs(got[k] - ref[k]).max() for k in ("vx", "vy", "vz")) <= 2e-4
+
+
+def test_bh_system_matches_plain_bh(nb):
+    s = nb.ics.plummer(12000, seed=31)
+    res, _ = _run(nb, {"b": (s, 30)}, direct_config=0)
+    got = res["b"][1]
+    calc = nb.BarnesHutCalculator(0.5)
+    calc.setSofteningParameter(0.01)
+    sysm = nb.System(calc, s)
+    sysm.step(1e-3, 30)
+    plain = sysm.read_f64()
+    sysm.close()
+    calc.close()
+    # same tree and walk; only the velocity-kick grouping differs
+    assert max(np.abs(got[k] - plain[k]).max() for k in ("x", "y", "z")) <= 1e-6
+
+
+def test_budget_and_resident_cap(nb):
+    from nbgb.serving import Ensemble
+    # a budget that fits about two 4096-body direct systems at a time
+    ens = Ensemble(hbm_budget_bytes=(1 << 20) * 4, max_resident=3, direct_config=0)
+    ids = [ens.submit(nb.ics.plummer(4096, seed=40 + k), 5, 1e-3) for k in range(6)]
+    peak_res, done = 0, []
+    for _ in range(200):
+        r, q = ens.tick()
+        peak_res = max(peak_res, r)
+        st = ens.stats()
+        assert st["bytes_reserved"] <= 4 * (1 << 20)
+        while True:
+            got = ens.poll()
+            if got is None:
+                break
+            done.append(got[0]["request_id"])
+        if len(done) == len(ids):
+            break
+    assert sorted(done) == sorted(ids)
+    assert 1 <= peak_res <= 3
+    assert ens.stats()["bytes_reserved"] == 0
+    ens.close()
+
+
+def test_oversized_request_rejected(nb):
+    from nbgb.serving import Ensemble
+    ens = Ensemble(hbm_budget_bytes=1 << 20)
+    with pytest.raises(nb.ResourceException):
+        ens.submit(nb.ics.plummer(65536, seed=1), 5, 1e-3)
+    ens.close()
+
+
+def test_autotuner_settles(nb):
+    from nbgb.serving import Ensemble
+    ens = Ensemble(hbm_budget_bytes=2 << 30)
+    for k in range(24):
+        ens.submit(nb.ics.plummer(1024 + 256 * k, seed=60 + k), 200, 1e-3)
+    for _ in range(40):
+        ens.tick()
+    st = ens.stats()
+    assert st["tuning"] == 0 and 0 <= st["direct_config"] < 6
+    assert st["direct_kernel_ms"] > 0 and st["direct_kernel_interactions"] > 0
+    ens.close()
