@@ -182,6 +182,7 @@ def gpu_arm(args, rank, world, local):
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with Clocks(dev_index) as clk:
+        torch.cuda.nvtx.range_push("bench_timed")  # profilers can filter on this range
         e0.record(est)
         t_host = time.perf_counter()
         for _ in range(args.steps):
@@ -189,6 +190,7 @@ def gpu_arm(args, rank, world, local):
         e1.record(est)
         torch.cuda.synchronize()
         host_s = time.perf_counter() - t_host
+        torch.cuda.nvtx.range_pop()
     elapsed_s = e0.elapsed_time(e1) / 1e3
     s1 = ens.stats()
     ps = s1["particle_steps"] - s0["particle_steps"]

@@ -246,6 +246,34 @@ struct ResidentSystem {
   int64_t graph_kernels = 0;  // kernel nodes in the captured step graph
 };
 
+// Host-to-device table uploads: the host runs ahead of the device, so a
+// pinned source buffer may only be rewritten after the copy that read it
+// has executed.  Each upload takes the next of kRing buffers and first waits
+// for the event recorded after that buffer's previous copy.
+struct UploadRing {
+  static constexpr int kRing = 8;
+  HostPinned<char> buf[kRing];
+  cudaEvent_t ev[kRing] = {};
+  bool used[kRing] = {};
+  int next = 0;
+  int cur = -1;
+  void* acquire(size_t bytes) {
+    cur = next++ % kRing;
+    if (used[cur]) NBGB_CUDA(cudaEventSynchronize(ev[cur]));
+    if (!ev[cur]) NBGB_CUDA(cudaEventCreateWithFlags(&ev[cur], cudaEventDisableTiming));
+    return buf[cur].ensure(std::max<size_t>(bytes, 1));
+  }
+  void upload(void* dst, size_t bytes, cudaStream_t st) {
+    if (bytes) NBGB_CUDA(cudaMemcpyAsync(dst, buf[cur].ptr, bytes, cudaMemcpyHostToDevice, st));
+    NBGB_CUDA(cudaEventRecord(ev[cur], st));
+    used[cur] = true;
+  }
+  ~UploadRing() {
+    for (int k = 0; k < kRing; ++k)
+      if (ev[k]) cudaEventDestroy(ev[k]);
+  }
+};
+
 struct Retiring {
   nbgb_ensemble_result res;
   std::unique_ptr<ResidentSystem> sys;
@@ -280,9 +308,7 @@ struct nbgb_ensemble {
   DevBuf<uint32_t> d_counter;
   DevBuf<uint32_t> d_err;
   DevBuf<float4> part;  // a(0) of direct systems: j-split partials
-  HostPinned<KDBlock> h_kd;
-  HostPinned<SlotParams> h_slot;
-  HostPinned<DirectItem> h_items;
+  UploadRing up_kd, up_slot, up_items;
   int n_kd = 0, n_items = 0;
   bool tables_dirty = true;
   int items_config = -1;
@@ -364,7 +390,7 @@ static void rebuild_tables(nbgb_ensemble* e) {
   // KD blocks (one per 256 bodies of every resident system)
   int64_t nb = 0;
   for (auto& s : e->resident) nb += s->n_pad / kChunk;
-  KDBlock* kd = e->h_kd.ensure((size_t)std::max<int64_t>(nb, 1));
+  KDBlock* kd = static_cast<KDBlock*>(e->up_kd.acquire((size_t)std::max<int64_t>(nb, 1) * sizeof(KDBlock)));
   int64_t b = 0;
   for (auto& s : e->resident) {
     for (int64_t c = 0; c < s->n_pad / kChunk; ++c) {
@@ -374,7 +400,7 @@ static void rebuild_tables(nbgb_ensemble* e) {
   }
   e->n_kd = (int)nb;
   KDBlock* dkd = e->d_kd.ensure((size_t)std::max<int64_t>(nb, 1));
-  if (nb) NBGB_CUDA(cudaMemcpyAsync(dkd, kd, (size_t)nb * sizeof(KDBlock), cudaMemcpyHostToDevice, e->main));
+  e->up_kd.upload(dkd, (size_t)nb * sizeof(KDBlock), e->main);
   // direct work items, largest systems first (longest-processing-time order)
   const DirectConfig& dc = kConfigs[e->config];
   const int ti = dc.threads * dc.per_thread;
@@ -384,13 +410,13 @@ static void rebuild_tables(nbgb_ensemble* e) {
   std::stable_sort(ds.begin(), ds.end(), [](auto* a, auto* b2) { return a->n > b2->n; });
   int64_t ni = 0;
   for (auto* s : ds) ni += ceil_div(s->n, ti);
-  DirectItem* it = e->h_items.ensure((size_t)std::max<int64_t>(ni, 1));
+  DirectItem* it = static_cast<DirectItem*>(e->up_items.acquire((size_t)std::max<int64_t>(ni, 1) * sizeof(DirectItem)));
   int64_t k = 0;
   for (auto* s : ds)
     for (int64_t f = 0; f < s->n; f += ti) it[k++] = DirectItem{s->off, (int32_t)s->n, (int32_t)f};
   e->n_items = (int)ni;
   DirectItem* dit = e->d_items.ensure((size_t)std::max<int64_t>(ni, 1));
-  if (ni) NBGB_CUDA(cudaMemcpyAsync(dit, it, (size_t)ni * sizeof(DirectItem), cudaMemcpyHostToDevice, e->main));
+  e->up_items.upload(dit, (size_t)ni * sizeof(DirectItem), e->main);
   e->items_config = e->config;
   e->tables_dirty = false;
 }
@@ -664,11 +690,11 @@ static void run_tick(nbgb_ensemble* e) {
   if (e->resident.empty()) return;
   if (e->tables_dirty || e->items_config != e->config) rebuild_tables(e);
   // per-slot kick factors
-  SlotParams* sp = e->h_slot.ensure((size_t)std::max(e->n_slots, 1));
+  SlotParams* sp = static_cast<SlotParams*>(e->up_slot.acquire((size_t)std::max(e->n_slots, 1) * sizeof(SlotParams)));
   for (auto& s : e->resident)
     sp[s->slot] = SlotParams{s->pending_half ? (double)s->dt : 0.5 * (double)s->dt, (double)s->dt};
   SlotParams* dsp = e->d_slot.ensure((size_t)std::max(e->n_slots, 1));
-  NBGB_CUDA(cudaMemcpyAsync(dsp, sp, (size_t)e->n_slots * sizeof(SlotParams), cudaMemcpyHostToDevice, e->main));
+  e->up_slot.upload(dsp, (size_t)e->n_slots * sizeof(SlotParams), e->main);
   // 1. kick-drift for everything resident
   if (e->n_kd) {
     const unsigned blocks = (unsigned)std::min(e->n_kd, num_sms() * 16);
