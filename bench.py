@@ -61,7 +61,48 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--case", choices=["direct", "bh", "bh8", "hash"], default=None,
+                    help="time one plain force evaluation of a single system instead "
+                         "(small profiling cases)")
+    ap.add_argument("--case-n", type=int, default=262144)
     return ap.parse_args()
+
+
+def case_arm(args, local):
+    """One system through nbgb_compute_forces: direct / Barnes-Hut (theta 0.5,
+    1 or 8 bodies per leaf) on a Plummer sphere, or the spatial hash on the
+    uniform cube at the serving density; prints ms per evaluation."""
+    import torch
+
+    import nbgb
+    torch.cuda.set_device(local)
+    n = args.case_n
+    if args.case == "hash":
+        side = 160.0 * (n / 4_194_304) ** (1.0 / 3.0)
+        s = nbgb.ics.uniform_cube(n, seed=3, side=side)
+        calc = nbgb.SpatialHashCalculator(2.0, 2.0)
+    elif args.case == "direct":
+        s = nbgb.ics.plummer(n, seed=1)
+        calc = nbgb.DirectForceCalculator()
+    else:
+        s = nbgb.ics.two_plummer(n, seed=2)
+        calc = nbgb.BarnesHutCalculator(0.5, leaf_capacity=8 if args.case == "bh8" else 1)
+    calc.setSofteningParameter(EPS)
+    st = torch.cuda.current_stream()
+    calc.set_stream(st.cuda_stream)
+    with nbgb.ScopedParticleData(n, {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"],
+                                     "mass": s["m"]}) as p:
+        for _ in range(max(args.warmup, 1)):
+            calc.computeForces(p.device)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            calc.computeForces(p.device)
+        e1.record(st)
+        torch.cuda.synchronize()
+    calc.close()
+    return {"case": args.case, "n": n, "ms_per_eval": e0.elapsed_time(e1) / args.steps}
 
 
 def dist_env():
@@ -428,7 +469,9 @@ def main() -> int:
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    if args.impl == "reference":
+    if args.case:
+        out = case_arm(args, local) if rank == 0 else None
+    elif args.impl == "reference":
         out = reference_arm(args, rank, world)
     else:
         out = gpu_arm(args, rank, world, local)
