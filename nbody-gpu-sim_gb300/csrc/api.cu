@@ -143,7 +143,8 @@ static DirectVariant default_variant() {
   const char* v = std::getenv("NBGB_DIRECT_VARIANT");
   if (v && std::strcmp(v, "scalar4") == 0) return DirectVariant::kScalar4;
   if (v && std::strcmp(v, "paired8") == 0) return DirectVariant::kPaired8;
-  return DirectVariant::kScalar4;
+  // packed FP32x2 halves the FP32 issue slots: 54.5 vs 48.5 TFLOP/s at N = 1M
+  return DirectVariant::kPaired8;
 }
 
 static void check_particles(const nbgb_particle_data* d, bool need_vel, bool need_old) {
