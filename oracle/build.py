@@ -92,6 +92,58 @@ def build_ref(force: bool = False) -> str | None:
     return REF_LIB
 
 
+def link_reference_apps(lib_dir: str) -> dict[str, str] | None:
+    """Link check of the drop-in: the reference's unchanged benchmark driver,
+    ParticleSystem, utilities and one example, with the hot-path classes
+    supplied by nbody-gpu-sim_gb300/adapter/nbody_adapter.cpp and the
+    kernels by libnbgb.so in lib_dir.  Outputs go to oracle/_ref/link/.
+    Returns {app: path} or None where the reference sources are absent."""
+    if not reference_available():
+        return None
+    repo = os.path.dirname(HERE)
+    out = os.path.join(REF_DIR, "link")
+    os.makedirs(out, exist_ok=True)
+    inc = ["-I", os.path.join(REF_ROOT, "include"), "-I", os.path.join(repo, "include"),
+           "-I", "/usr/local/cuda/include"]
+    defs = ["-DNDEBUG", "-DNBODY_WITH_CUDA=1", "-DNBODY_WITH_RENDERING=0", "-DNBODY_WITH_UI=0",
+            "-DNBODY_ENABLE_PROFILING=1"]
+    srcs = ["src/core/particle_system.cpp", "src/utils/error_handling.cpp",
+            "src/utils/performance_observability.cpp", "src/utils/serialization.cpp",
+            "src/utils/simulation_state.cpp"]
+    jobs, objs = [], []
+    for s in srcs:
+        o = os.path.join(out, os.path.basename(s) + ".o")
+        jobs.append(["g++", "-std=c++17", "-O2", "-fPIC"] + defs + inc +
+                    ["-c", os.path.join(REF_ROOT, s), "-o", o])
+        objs.append(o)
+    # particle_init.cu holds host code only (allocation, copies, initialisers)
+    o = os.path.join(out, "particle_init.cu.o")
+    jobs.append(["nvcc", "-std=c++17", "-O2", "-Xcompiler", "-fPIC",
+                 "-gencode", "arch=compute_103a,code=sm_103a"] + defs + inc +
+                ["-c", os.path.join(REF_ROOT, "src/cuda/particle_init.cu"), "-o", o])
+    objs.append(o)
+    ad = os.path.join(out, "nbody_adapter.o")
+    jobs.append(["g++", "-std=c++17", "-O2", "-fPIC"] + defs + inc +
+                ["-c", os.path.join(repo, "nbody-gpu-sim_gb300", "adapter", "nbody_adapter.cpp"),
+                 "-o", ad])
+    objs.append(ad)
+    mains = {"nbody_benchmarks": "benchmarks/benchmark_main.cpp",
+             "example_basic": "examples/example_basic.cpp"}
+    for app, s in mains.items():
+        jobs.append(["g++", "-std=c++17", "-O2", "-fPIC"] + defs + inc +
+                    ["-c", os.path.join(REF_ROOT, s), "-o", os.path.join(out, app + ".o")])
+    with ThreadPoolExecutor(max_workers=8) as ex:
+        list(ex.map(_run, jobs))
+    apps = {}
+    for app in mains:
+        exe = os.path.join(out, app)
+        _run(["g++", "-o", exe, os.path.join(out, app + ".o")] + objs +
+             ["-L", lib_dir, "-lnbgb", "-Wl,-rpath," + lib_dir, "-L", "/usr/local/cuda/lib64",
+              "-lcudart", "-lpthread"])
+        apps[app] = exe
+    return apps
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     if "--ref" in sys.argv:
