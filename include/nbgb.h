@@ -128,6 +128,22 @@ nbgb_status nbgb_calculator_synchronize(nbgb_calculator* calc);
  * OVERWRITES acc_x/y/z, touches nothing else.  Device pointers. */
 nbgb_status nbgb_compute_forces(nbgb_calculator* calc, const nbgb_particle_data* d_particles);
 
+/* Direct-sum forces that allocate no device memory (no counterpart in the
+ * reference).  For callers that may not call cudaMalloc/cudaFree -- e.g. a
+ * host application that owns all device memory through its own pool, or a
+ * latency-critical loop that cannot afford cudaMalloc's implicit device
+ * synchronisation.  Same contract as nbgb_compute_forces with a direct
+ * calculator of the given G and softening: reads pos_x/y/z and mass, writes
+ * acc_x/y/z (device pointers), compensated FP32 sums.  Limit: count <=
+ * 65536 (larger counts return NBGB_ERR_INVALID_ARG).  Scratch is ~9 MiB of
+ * static device memory per device, held from library load until exit; the
+ * first call on a device resolves its address (make that first call before
+ * any stream capture).  All calls share that scratch: calls that overlap on
+ * the GPU race and must be serialised by the caller.  Work is enqueued on
+ * `stream` (NULL = legacy default stream) and the call waits for it. */
+nbgb_status nbgb_compute_forces_direct_noalloc(const nbgb_particle_data* d_particles, float G,
+                                               float softening, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Integrator (include/nbody/integrator.hpp:15-33, src/cuda/integrator.cu).
  * FP32 SoA semantics of the reference; device pointers.
