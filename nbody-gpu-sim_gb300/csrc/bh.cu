@@ -69,6 +69,7 @@ struct BHState {
   int64_t n = 0;
   int64_t cap = 0;
   bool m_alt = false;      // Morton result in *_alt
+  bool keys_valid = false; // Morton (key, index) pairs computed for the last build
   const uint32_t* body = nullptr;  // path-sorted body indices
   const u64* hi_sorted = nullptr;
 };
@@ -181,6 +182,73 @@ __global__ void path_final_kernel(const float4* __restrict__ pm, const uint32_t*
     path_key(p, b, h, l);
     lo[k] = l;
     spm[k] = p;
+  }
+}
+
+// High path key of every body in index order (values = body indices).
+__global__ void path_hi_index_kernel(const float4* __restrict__ pm, int64_t n,
+                                     const BBox* __restrict__ box, u64* __restrict__ hi,
+                                     uint32_t* __restrict__ idx) {
+  const BBox b = *box;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    u64 h, l;
+    path_key(pm[i], b, h, l);
+    hi[i] = h;
+    idx[i] = (uint32_t)i;
+  }
+}
+
+// Tie key of a body: low path key, then Morton key, then index.
+__device__ __forceinline__ bool tie_less(const float4* __restrict__ pm, const BBox& b, uint32_t a,
+                                         uint32_t c) {
+  u64 ha, la, hc, lc;
+  const float4 pa = pm[a], pc = pm[c];
+  path_key(pa, b, ha, la);
+  path_key(pc, b, hc, lc);
+  if (la != lc) return la < lc;
+  const uint32_t ma = morton_of(pa, b), mc = morton_of(pc, b);
+  if (ma != mc) return ma < mc;
+  return a < c;
+}
+
+// Runs of equal high keys (bodies sharing their first 21 octants; tiny in
+// practice) are put in (low key, Morton key, index) order by one thread per
+// run with an insertion sort.  A run that is already in order (e.g. many
+// coincident bodies) costs one comparison per body.
+__global__ void tie_order_kernel(const float4* __restrict__ pm, int64_t n,
+                                 const BBox* __restrict__ box, const u64* __restrict__ hi,
+                                 uint32_t* __restrict__ body) {
+  const BBox b = *box;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k + 1 < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    if (k > 0 && hi[k - 1] == hi[k]) continue;  // not the start of a run
+    if (hi[k + 1] != hi[k]) continue;           // run of one
+    int64_t e = k + 1;
+    while (e + 1 < n && hi[e + 1] == hi[k]) ++e;
+    for (int64_t i = k + 1; i <= e; ++i) {
+      const uint32_t cur = body[i];
+      int64_t j = i - 1;
+      while (j >= k && tie_less(pm, b, cur, body[j])) {
+        body[j + 1] = body[j];
+        --j;
+      }
+      body[j + 1] = cur;
+    }
+  }
+}
+
+// Morton keys scattered back to index order (for the on-demand key sort).
+__global__ void morton_scatter_kernel(const float4* __restrict__ spm,
+                                      const uint32_t* __restrict__ body, int64_t n,
+                                      const BBox* __restrict__ box, uint32_t* __restrict__ keys,
+                                      uint32_t* __restrict__ idx) {
+  const BBox b = *box;
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t i = body[k];
+    keys[i] = morton_of(spm[k], b);
+    idx[i] = i;
   }
 }
 
@@ -400,6 +468,20 @@ struct WalkArgs {
   int32_t* counts;
 };
 
+// The reference's opening test `size2 / dist2 < theta2` with the correctly
+// rounded quotient (force_barnes_hut.cu:222-224), decided from the MUFU
+// reciprocal whenever the approximate quotient is far (2^-16 relative) from
+// the threshold, which is almost always; only the near-threshold cases pay
+// for the IEEE division.  The outcome equals the IEEE comparison.
+__device__ __forceinline__ bool opening_accept(float size2, float d2, float theta2) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d2));
+  const float q = size2 * r;
+  if (q < theta2 * (1.0f - 1.52587890625e-05f)) return true;
+  if (q > theta2 * (1.0f + 1.52587890625e-05f)) return false;
+  return __fdiv_rn(size2, d2) < theta2;
+}
+
 __device__ __forceinline__ void bh_add(float px, float py, float pz, float m, float xi, float yi,
                                        float zi, float eps2, float& sx, float& sy, float& sz) {
   const float dx = __fsub_rn(px, xi), dy = __fsub_rn(py, yi), dz = __fsub_rn(pz, zi);
@@ -463,7 +545,7 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
                   dz = __fsub_rn(cm.z, pi.z);
       const float d2 = __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), a.eps2);
       const float size2 = __fmul_rn(__fmul_rn(4.0f, g.w), g.w);
-      const bool accept = !contains && (__fdiv_rn(size2, d2) < a.theta2);
+      const bool accept = !contains && opening_accept(size2, d2, a.theta2);
       const bool open = active && !accept;
       if (active && accept) {
         const float r = rsqrt_approx(d2);
@@ -499,6 +581,120 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
   }
 }
 
+// Group walk (leaf_capacity > 1).  A warp owns 32 consecutive targets in
+// path order and walks the tree once for all of them: a cell is accepted as
+// a point mass when it does not overlap the targets' bounding box and
+// 4h^2 / (d_min^2 + eps^2) < theta^2 for the box's nearest point (so every
+// target of the group would accept it under the per-target rule); a cell
+// holding at most leaf_capacity bodies that is not accepted contributes its
+// bodies one by one; anything else is opened.  Accepted cells and bodies go
+// to a per-warp shared-memory list that all 32 lanes then sum like a direct
+// j-tile (broadcast loads, no divergence).  A target's own body in a list
+// contributes exactly 0 (d = 0, eps > 0).
+constexpr int kGroupList = 64;
+
+template <bool COUNT, bool ZERO_SOFT>
+__device__ __forceinline__ void group_flush(const float4* __restrict__ list, int len, float4 pi,
+                                            float eps2, float& sx, float& sy, float& sz,
+                                            int& cnt) {
+  __syncwarp();
+#pragma unroll 4
+  for (int e = 0; e < len; ++e) {
+    const float4 p = list[e];
+    const float dx = p.x - pi.x, dy = p.y - pi.y, dz = p.z - pi.z;
+    const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
+    float r = rsqrt_approx(d2);
+    if constexpr (ZERO_SOFT) r = (d2 > 0.f) ? r : 0.f;
+    const float f = (p.w * r) * (r * r);
+    sx = fmaf(f, dx, sx);
+    sy = fmaf(f, dy, sy);
+    sz = fmaf(f, dz, sz);
+  }
+  if (COUNT) cnt += len;
+  __syncwarp();
+}
+
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <bool COUNT, bool ZERO_SOFT>
+__global__ void __launch_bounds__(256) bh_group_walk_kernel(WalkArgs a) {
+  __shared__ alignas(16) float4 s_list[256 / 32][kGroupList];
+  const uint32_t total = a.nstart[a.n];
+  const bool tree_ok = (int64_t)total <= a.cap;
+  const int lane = threadIdx.x & 31;
+  float4* list = s_list[threadIdx.x >> 5];
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t wbase = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < a.n;
+       wbase += warps * 32) {
+    const int64_t k = wbase + lane;
+    const bool valid = k < a.n;
+    const float4 pi = a.spm[valid ? k : wbase];
+    const float lox = warp_min(pi.x), hix = warp_max(pi.x);
+    const float loy = warp_min(pi.y), hiy = warp_max(pi.y);
+    const float loz = warp_min(pi.z), hiz = warp_max(pi.z);
+    const float gcx = 0.5f * (lox + hix), gcy = 0.5f * (loy + hiy), gcz = 0.5f * (loz + hiz);
+    const float ghx = 0.5f * (hix - lox), ghy = 0.5f * (hiy - loy), ghz = 0.5f * (hiz - loz);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    int cnt = 0, len = 0;
+    int node = tree_ok ? 0 : (int)total;
+    while (node < (int)total) {
+      const float4 cm = a.com[node];
+      const int4 in = a.info[node];
+      if (cm.w == 0.0f) {
+        node = in.x;
+        continue;
+      }
+      const float4 g = a.geom[node];
+      const bool overlap = fabsf(g.x - gcx) <= g.w + ghx && fabsf(g.y - gcy) <= g.w + ghy &&
+                           fabsf(g.z - gcz) <= g.w + ghz;
+      const float ex = fmaxf(fmaxf(lox - cm.x, cm.x - hix), 0.f);
+      const float ey = fmaxf(fmaxf(loy - cm.y, cm.y - hiy), 0.f);
+      const float ez = fmaxf(fmaxf(loz - cm.z, cm.z - hiz), 0.f);
+      const float d2min = fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, a.eps2)));
+      const bool accept = !overlap && (4.0f * g.w) * g.w < a.theta2 * d2min;
+      if (accept) {
+        if (lane == 0) list[len] = cm;
+        ++len;
+        node = in.x;
+      } else if ((in.w & 1) || in.z <= a.leaf_cap) {
+        for (int base = 0; base < in.z; base += 32) {
+          const int m = min(32, in.z - base);
+          if (lane < m) list[len + lane] = a.spm[(int64_t)in.y + base + lane];
+          len += m;
+          if (len >= 32) {
+            group_flush<COUNT, ZERO_SOFT>(list, len, pi, a.eps2, sx, sy, sz, cnt);
+            len = 0;
+          }
+        }
+        node = in.x;
+      } else {
+        node = node + 1;
+      }
+      if (len >= 32) {
+        group_flush<COUNT, ZERO_SOFT>(list, len, pi, a.eps2, sx, sy, sz, cnt);
+        len = 0;
+      }
+    }
+    if (len) group_flush<COUNT, ZERO_SOFT>(list, len, pi, a.eps2, sx, sy, sz, cnt);
+    if (valid) {
+      const uint32_t i = a.body[k];
+      a.ax[i] = a.G * sx;
+      a.ay[i] = a.G * sy;
+      a.az[i] = a.G * sz;
+      if (COUNT) a.counts[i] = cnt;
+    }
+  }
+}
+
 static unsigned grid1d(int64_t n, int threads = 256) {
   return (unsigned)std::max<int64_t>(
       1, std::min<int64_t>(ceil_div(std::max<int64_t>(n, 1), threads), (int64_t)num_sms() * 32));
@@ -513,37 +709,27 @@ static void bh_build(nbgb_calculator* c, BHState& h, const float4* pm, int64_t n
   float* part = h.bbox_part.ensure((size_t)bbox_blocks(n) * 6);
   BBox* box = h.box.ensure(1);
   launch_bbox(pm, n, part, box, err, st);
-  // Morton keys + stable sort (bit-exact with the reference's keys and order)
-  uint32_t* mk = h.mkeys.ensure((size_t)n);
-  uint32_t* mi = h.midx.ensure((size_t)n);
-  uint32_t* mk2 = h.mkeys_alt.ensure((size_t)n);
-  uint32_t* mi2 = h.midx_alt.ensure((size_t)n);
   uint32_t* hist = h.hist.ensure(radix_hist_elems(n));
   uint32_t* sws = h.scan_ws.ensure(scan_workspace_elems((int64_t)radix_hist_elems(n)) +
                                    scan_workspace_elems(n + 1));
-  morton_kernel<<<grid1d(n), 256, 0, st>>>(pm, n, box, mk, mi);
-  NBGB_LAUNCH_CHECK();
-  radix_sort_pairs<uint32_t>(mk, mk2, mi, mi2, n, 0, 32, hist, sws, st, &h.m_alt);
-  const uint32_t* morton_body = h.m_alt ? mi2 : mi;
-  // path keys: sort by low levels, then (stably) by high levels
+  // Path keys in index order, stable radix sort by the high key (levels
+  // 1..21, 8 passes), then bodies that share their high key are ordered by
+  // (low key, Morton key, index): the full path order with the reference's
+  // insertion order (stable Morton order) inside a shared depth-32 cell.
   u64* lo = h.klo.ensure((size_t)n);
-  u64* lo2 = h.klo_alt.ensure((size_t)n);
   u64* hi = h.khi.ensure((size_t)n);
   u64* hi2 = h.khi_alt.ensure((size_t)n);
   uint32_t* pb = h.pidx.ensure((size_t)n);
   uint32_t* pb2 = h.pidx_alt.ensure((size_t)n);
-  path_lo_kernel<<<grid1d(n), 256, 0, st>>>(pm, morton_body, n, box, lo, pb);
+  path_hi_index_kernel<<<grid1d(n), 256, 0, st>>>(pm, n, box, hi, pb);
   NBGB_LAUNCH_CHECK();
   bool alt = false;
-  radix_sort_pairs<u64>(lo, lo2, pb, pb2, n, 0, 40, hist, sws, st, &alt);
-  uint32_t* b1 = alt ? pb2 : pb;
-  uint32_t* b1_other = alt ? pb : pb2;
-  path_hi_kernel<<<grid1d(n), 256, 0, st>>>(pm, b1, n, box, hi);
+  radix_sort_pairs<u64>(hi, hi2, pb, pb2, n, 0, 64, hist, sws, st, &alt);
+  h.body = alt ? pb2 : pb;
+  h.hi_sorted = alt ? hi2 : hi;
+  tie_order_kernel<<<grid1d(n), 256, 0, st>>>(pm, n, box, h.hi_sorted, const_cast<uint32_t*>(h.body));
   NBGB_LAUNCH_CHECK();
-  bool alt2 = false;
-  radix_sort_pairs<u64>(hi, hi2, b1, b1_other, n, 0, 64, hist, sws, st, &alt2);
-  h.body = alt2 ? b1_other : b1;
-  h.hi_sorted = alt2 ? hi2 : hi;
+  h.keys_valid = false;  // Morton (key, index) pairs are produced on demand
   float4* spm = h.spm.ensure((size_t)n);
   path_final_kernel<<<grid1d(n), 256, 0, st>>>(pm, h.body, n, box, lo, spm);
   NBGB_LAUNCH_CHECK();
@@ -627,13 +813,18 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
   w.az = az;
   const bool count = (c->params.flags & NBGB_FLAG_COUNT_INTERACTIONS) != 0;
   w.counts = count ? c->counts.ensure((size_t)n) : nullptr;
-  const bool bucket = c->params.leaf_capacity > 1;
+  const bool group = c->params.leaf_capacity > 1;
+  const bool zs = !(w.eps2 > 0.f);
   const unsigned blocks = grid1d(n);
-  if (count) {
-    if (bucket) bh_walk_kernel<true, true><<<blocks, 256, 0, st>>>(w);
-    else bh_walk_kernel<true, false><<<blocks, 256, 0, st>>>(w);
+  if (group) {
+    if (count)
+      zs ? bh_group_walk_kernel<true, true><<<blocks, 256, 0, st>>>(w)
+         : bh_group_walk_kernel<true, false><<<blocks, 256, 0, st>>>(w);
+    else
+      zs ? bh_group_walk_kernel<false, true><<<blocks, 256, 0, st>>>(w)
+         : bh_group_walk_kernel<false, false><<<blocks, 256, 0, st>>>(w);
   } else {
-    if (bucket) bh_walk_kernel<false, true><<<blocks, 256, 0, st>>>(w);
+    if (count) bh_walk_kernel<true, false><<<blocks, 256, 0, st>>>(w);
     else bh_walk_kernel<false, false><<<blocks, 256, 0, st>>>(w);
   }
   NBGB_LAUNCH_CHECK();
@@ -704,6 +895,25 @@ nbgb_status nbgb_bh_copy_sorted_keys(nbgb_calculator* c, uint32_t* keys, int32_t
   if (!c || !c->bh || c->method != NBGB_BARNES_HUT) return NBGB_ERR_INVALID_ARG;
   BHState& h = *c->bh;
   if (n != (size_t)h.n) return NBGB_ERR_INVALID_ARG;
+  if (!h.keys_valid) {
+    // The reference's Morton keys and their stable sort
+    // (force_barnes_hut.cu:308-328), from the bodies of the last build.
+    try {
+      const int64_t nn = h.n;
+      uint32_t* mk = h.mkeys.ensure((size_t)nn);
+      uint32_t* mi = h.midx.ensure((size_t)nn);
+      uint32_t* mk2 = h.mkeys_alt.ensure((size_t)nn);
+      uint32_t* mi2 = h.midx_alt.ensure((size_t)nn);
+      morton_scatter_kernel<<<grid1d(nn), 256, 0, c->stream>>>(h.spm.ptr, h.body, nn, h.box.ptr,
+                                                              mk, mi);
+      NBGB_LAUNCH_CHECK();
+      radix_sort_pairs<uint32_t>(mk, mk2, mi, mi2, nn, 0, 32, h.hist.ptr, h.scan_ws.ptr,
+                                 c->stream, &h.m_alt);
+      h.keys_valid = true;
+    } catch (const Error& e) {
+      return e.status;
+    }
+  }
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return NBGB_ERR_CUDA;
   const uint32_t* k = h.m_alt ? h.mkeys_alt.ptr : h.mkeys.ptr;
   const uint32_t* v = h.m_alt ? h.midx_alt.ptr : h.midx.ptr;
