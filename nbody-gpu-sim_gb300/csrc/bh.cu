@@ -493,19 +493,12 @@ __device__ __forceinline__ void bh_add(float px, float py, float pz, float m, fl
   sz = fmaf(f, dz, sz);
 }
 
+// One warp, 32 targets, each lane applying the reference's per-target rules
+// (union traversal; see the file header).  Adds into sx/sy/sz/cnt.
 template <bool COUNT, bool BUCKET>
-__global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
-  const uint32_t total = a.nstart[a.n];
-  const bool tree_ok = (int64_t)total <= a.cap;
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t wbase = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < a.n;
-       wbase += warps * 32) {
-    const int64_t k = wbase + lane;
-    const bool valid = k < a.n;
-    const float4 pi = valid ? a.spm[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    int cnt = 0;
+__device__ __forceinline__ void lane_walk(const WalkArgs& a, int64_t k, bool valid, float4 pi,
+                                          uint32_t total, bool tree_ok, float& sx, float& sy,
+                                          float& sz, int& cnt) {
     int resume = valid ? 0 : 0x7fffffff;
     int node = tree_ok ? 0 : (int)total;
     while (node < (int)total) {
@@ -571,6 +564,22 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
       }
       node = __any_sync(0xffffffffu, open) ? node + 1 : in.x;
     }
+}
+
+template <bool COUNT, bool BUCKET>
+__global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
+  const uint32_t total = a.nstart[a.n];
+  const bool tree_ok = (int64_t)total <= a.cap;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t wbase = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < a.n;
+       wbase += warps * 32) {
+    const int64_t k = wbase + lane;
+    const bool valid = k < a.n;
+    const float4 pi = valid ? a.spm[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    int cnt = 0;
+    lane_walk<COUNT, BUCKET>(a, k, valid, pi, total, tree_ok, sx, sy, sz, cnt);
     if (valid) {
       const uint32_t i = a.body[k];
       a.ax[i] = a.G * sx;
@@ -592,6 +601,7 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
 // j-tile (broadcast loads, no divergence).  A target's own body in a list
 // contributes exactly 0 (d = 0, eps > 0).
 constexpr int kGroupList = 64;
+constexpr int kGroupBudget = 8192;  // list entries before a group falls back to per-target walks
 
 template <bool COUNT, bool ZERO_SOFT>
 __device__ __forceinline__ void group_flush(const float4* __restrict__ list, int len, float4 pi,
@@ -644,9 +654,10 @@ __global__ void __launch_bounds__(256) bh_group_walk_kernel(WalkArgs a) {
     const float gcx = 0.5f * (lox + hix), gcy = 0.5f * (loy + hiy), gcz = 0.5f * (loz + hiz);
     const float ghx = 0.5f * (hix - lox), ghy = 0.5f * (hiy - loy), ghz = 0.5f * (hiz - loz);
     float sx = 0.f, sy = 0.f, sz = 0.f;
-    int cnt = 0, len = 0;
+    int cnt = 0, len = 0, listed = 0;
     int node = tree_ok ? 0 : (int)total;
     while (node < (int)total) {
+      if (listed > kGroupBudget) break;  // spread-out group: per-target walk below
       const float4 cm = a.com[node];
       const int4 in = a.info[node];
       if (cm.w == 0.0f) {
@@ -664,12 +675,14 @@ __global__ void __launch_bounds__(256) bh_group_walk_kernel(WalkArgs a) {
       if (accept) {
         if (lane == 0) list[len] = cm;
         ++len;
+        ++listed;
         node = in.x;
       } else if ((in.w & 1) || in.z <= a.leaf_cap) {
         for (int base = 0; base < in.z; base += 32) {
           const int m = min(32, in.z - base);
           if (lane < m) list[len + lane] = a.spm[(int64_t)in.y + base + lane];
           len += m;
+          listed += m;
           if (len >= 32) {
             group_flush<COUNT, ZERO_SOFT>(list, len, pi, a.eps2, sx, sy, sz, cnt);
             len = 0;
@@ -684,7 +697,17 @@ __global__ void __launch_bounds__(256) bh_group_walk_kernel(WalkArgs a) {
         len = 0;
       }
     }
-    if (len) group_flush<COUNT, ZERO_SOFT>(list, len, pi, a.eps2, sx, sy, sz, cnt);
+    if (listed > kGroupBudget) {
+      // The group box is too spread out (sparse outskirts, or 32 targets
+      // straddling distant cells): the shared list would grow towards N.
+      // Redo this warp with each lane's own criterion (bounded cost).
+      __syncwarp();
+      sx = sy = sz = 0.f;
+      cnt = 0;
+      lane_walk<COUNT, true>(a, k, valid, pi, total, tree_ok, sx, sy, sz, cnt);
+    } else if (len) {
+      group_flush<COUNT, ZERO_SOFT>(list, len, pi, a.eps2, sx, sy, sz, cnt);
+    }
     if (valid) {
       const uint32_t i = a.body[k];
       a.ax[i] = a.G * sx;
