@@ -590,134 +590,6 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
   }
 }
 
-// Group walk (leaf_capacity > 1).  A warp owns 32 consecutive targets in
-// path order and walks the tree once for all of them: a cell is accepted as
-// a point mass when it does not overlap the targets' bounding box and
-// 4h^2 / (d_min^2 + eps^2) < theta^2 for the box's nearest point (so every
-// target of the group would accept it under the per-target rule); a cell
-// holding at most leaf_capacity bodies that is not accepted contributes its
-// bodies one by one; anything else is opened.  Accepted cells and bodies go
-// to a per-warp shared-memory list that all 32 lanes then sum like a direct
-// j-tile (broadcast loads, no divergence).  A target's own body in a list
-// contributes exactly 0 (d = 0, eps > 0).
-constexpr int kGroupList = 64;
-constexpr int kGroupBudget = 8192;  // list entries before a group falls back to per-target walks
-
-template <bool COUNT, bool ZERO_SOFT>
-__device__ __forceinline__ void group_flush(const float4* __restrict__ list, int len, float4 pi,
-                                            float eps2, float& sx, float& sy, float& sz,
-                                            int& cnt) {
-  __syncwarp();
-#pragma unroll 4
-  for (int e = 0; e < len; ++e) {
-    const float4 p = list[e];
-    const float dx = p.x - pi.x, dy = p.y - pi.y, dz = p.z - pi.z;
-    const float d2 = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-    float r = rsqrt_approx(d2);
-    if constexpr (ZERO_SOFT) r = (d2 > 0.f) ? r : 0.f;
-    const float f = (p.w * r) * (r * r);
-    sx = fmaf(f, dx, sx);
-    sy = fmaf(f, dy, sy);
-    sz = fmaf(f, dz, sz);
-  }
-  if (COUNT) cnt += len;
-  __syncwarp();
-}
-
-__device__ __forceinline__ float warp_min(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-__device__ __forceinline__ float warp_max(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-
-template <bool COUNT, bool ZERO_SOFT>
-__global__ void __launch_bounds__(256) bh_group_walk_kernel(WalkArgs a) {
-  __shared__ alignas(16) float4 s_list[256 / 32][kGroupList];
-  const uint32_t total = a.nstart[a.n];
-  const bool tree_ok = (int64_t)total <= a.cap;
-  const int lane = threadIdx.x & 31;
-  float4* list = s_list[threadIdx.x >> 5];
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t wbase = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < a.n;
-       wbase += warps * 32) {
-    const int64_t k = wbase + lane;
-    const bool valid = k < a.n;
-    const float4 pi = a.spm[valid ? k : wbase];
-    const float lox = warp_min(pi.x), hix = warp_max(pi.x);
-    const float loy = warp_min(pi.y), hiy = warp_max(pi.y);
-    const float loz = warp_min(pi.z), hiz = warp_max(pi.z);
-    const float gcx = 0.5f * (lox + hix), gcy = 0.5f * (loy + hiy), gcz = 0.5f * (loz + hiz);
-    const float ghx = 0.5f * (hix - lox), ghy = 0.5f * (hiy - loy), ghz = 0.5f * (hiz - loz);
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    int cnt = 0, len = 0, listed = 0;
-    int node = tree_ok ? 0 : (int)total;
-    while (node < (int)total) {
-      if (listed > kGroupBudget) break;  // spread-out group: per-target walk below
-      const float4 cm = a.com[node];
-      const int4 in = a.info[node];
-      if (cm.w == 0.0f) {
-        node = in.x;
-        continue;
-      }
-      const float4 g = a.geom[node];
-      const bool overlap = fabsf(g.x - gcx) <= g.w + ghx && fabsf(g.y - gcy) <= g.w + ghy &&
-                           fabsf(g.z - gcz) <= g.w + ghz;
-      const float ex = fmaxf(fmaxf(lox - cm.x, cm.x - hix), 0.f);
-      const float ey = fmaxf(fmaxf(loy - cm.y, cm.y - hiy), 0.f);
-      const float ez = fmaxf(fmaxf(loz - cm.z, cm.z - hiz), 0.f);
-      const float d2min = fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, a.eps2)));
-      const bool accept = !overlap && (4.0f * g.w) * g.w < a.theta2 * d2min;
-      if (accept) {
-        if (lane == 0) list[len] = cm;
-        ++len;
-        ++listed;
-        node = in.x;
-      } else if ((in.w & 1) || in.z <= a.leaf_cap) {
-        for (int base = 0; base < in.z; base += 32) {
-          const int m = min(32, in.z - base);
-          if (lane < m) list[len + lane] = a.spm[(int64_t)in.y + base + lane];
-          len += m;
-          listed += m;
-          if (len >= 32) {
-            group_flush<COUNT, ZERO_SOFT>(list, len, pi, a.eps2, sx, sy, sz, cnt);
-            len = 0;
-          }
-        }
-        node = in.x;
-      } else {
-        node = node + 1;
-      }
-      if (len >= 32) {
-        group_flush<COUNT, ZERO_SOFT>(list, len, pi, a.eps2, sx, sy, sz, cnt);
-        len = 0;
-      }
-    }
-    if (listed > kGroupBudget) {
-      // The group box is too spread out (sparse outskirts, or 32 targets
-      // straddling distant cells): the shared list would grow towards N.
-      // Redo this warp with each lane's own criterion (bounded cost).
-      __syncwarp();
-      sx = sy = sz = 0.f;
-      cnt = 0;
-      lane_walk<COUNT, true>(a, k, valid, pi, total, tree_ok, sx, sy, sz, cnt);
-    } else if (len) {
-      group_flush<COUNT, ZERO_SOFT>(list, len, pi, a.eps2, sx, sy, sz, cnt);
-    }
-    if (valid) {
-      const uint32_t i = a.body[k];
-      a.ax[i] = a.G * sx;
-      a.ay[i] = a.G * sy;
-      a.az[i] = a.G * sz;
-      if (COUNT) a.counts[i] = cnt;
-    }
-  }
-}
-
 static unsigned grid1d(int64_t n, int threads = 256) {
   return (unsigned)std::max<int64_t>(
       1, std::min<int64_t>(ceil_div(std::max<int64_t>(n, 1), threads), (int64_t)num_sms() * 32));
@@ -836,18 +708,13 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
   w.az = az;
   const bool count = (c->params.flags & NBGB_FLAG_COUNT_INTERACTIONS) != 0;
   w.counts = count ? c->counts.ensure((size_t)n) : nullptr;
-  const bool group = c->params.leaf_capacity > 1;
-  const bool zs = !(w.eps2 > 0.f);
+  const bool bucket = c->params.leaf_capacity > 1;
   const unsigned blocks = grid1d(n);
-  if (group) {
-    if (count)
-      zs ? bh_group_walk_kernel<true, true><<<blocks, 256, 0, st>>>(w)
-         : bh_group_walk_kernel<true, false><<<blocks, 256, 0, st>>>(w);
-    else
-      zs ? bh_group_walk_kernel<false, true><<<blocks, 256, 0, st>>>(w)
-         : bh_group_walk_kernel<false, false><<<blocks, 256, 0, st>>>(w);
+  if (count) {
+    if (bucket) bh_walk_kernel<true, true><<<blocks, 256, 0, st>>>(w);
+    else bh_walk_kernel<true, false><<<blocks, 256, 0, st>>>(w);
   } else {
-    if (count) bh_walk_kernel<true, false><<<blocks, 256, 0, st>>>(w);
+    if (bucket) bh_walk_kernel<false, true><<<blocks, 256, 0, st>>>(w);
     else bh_walk_kernel<false, false><<<blocks, 256, 0, st>>>(w);
   }
   NBGB_LAUNCH_CHECK();

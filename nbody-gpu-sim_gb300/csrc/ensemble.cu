@@ -798,7 +798,7 @@ void nbgb_ensemble_config_default(nbgb_ensemble_config* c) {
   c->G = 1.0f;
   c->softening = 0.01f;
   c->theta = 0.5f;
-  c->leaf_capacity = 8;  // group walk with 8-body buckets (1 = the reference's per-target walk)
+  c->leaf_capacity = 1;  // the reference's tree walk (8 = bodies of small subtrees summed directly)
   c->direct_config = -1;
   c->use_graphs = 1;
 }

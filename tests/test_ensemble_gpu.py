@@ -97,8 +97,7 @@ def test_bh_system_matches_plain_bh(nb):
     s = nb.ics.plummer(12000, seed=31)
     res, _ = _run(nb, {"b": (s, 30)}, direct_config=0)
     got = res["b"][1]
-    # the ensemble's Barnes-Hut systems use 8-body buckets (group walk)
-    calc = nb.BarnesHutCalculator(0.5, leaf_capacity=8)
+    calc = nb.BarnesHutCalculator(0.5)
     calc.setSofteningParameter(0.01)
     sysm = nb.System(calc, s)
     sysm.step(1e-3, 30)
