@@ -61,11 +61,31 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--case", choices=["direct", "bh", "bh8", "hash"], default=None,
+    ap.add_argument("--case", choices=["direct", "bh", "bh8", "hash", "precision"], default=None,
                     help="time one plain force evaluation of a single system instead "
-                         "(small profiling cases)")
+                         "(small profiling cases), or run the precision study")
     ap.add_argument("--case-n", type=int, default=262144)
+    ap.add_argument("--precision-steps", type=int, default=2000)
     return ap.parse_args()
+
+
+def precision_arm(args, local) -> dict:
+    """Precision study on a Plummer sphere (a=1, M=1), eps=1e-3, dt=2^-10:
+    force error of FP32 plain and FP32 compensated against the FP64 direct
+    sum at N=262144 (4096 seeded targets); energy drift over 2000 steps of
+    both FP32 variants at N=262144 and of all three variants (with full
+    FP64) at N=16384, where FP64 arithmetic fits the time budget."""
+    import torch
+
+    import nbgb.precision as prec
+    torch.cuda.set_device(local)
+    eps, dt = 1e-3, 2.0 ** -10
+    steps = args.precision_steps
+    out = {"case": "precision", "force_error": prec.force_errors(args.case_n, eps),
+           "energy_full_n": prec.energy_drift(args.case_n, eps, dt, steps,
+                                              variants=("fp32", "fp32c_fp64")),
+           "energy_small_n": prec.energy_drift(16384, eps, dt, steps)}
+    return out
 
 
 def case_arm(args, local):
@@ -469,7 +489,9 @@ def main() -> int:
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    if args.case:
+    if args.case == "precision":
+        out = precision_arm(args, local) if rank == 0 else None
+    elif args.case:
         out = case_arm(args, local) if rank == 0 else None
     elif args.impl == "reference":
         out = reference_arm(args, rank, world)

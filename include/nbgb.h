@@ -99,6 +99,10 @@ typedef struct nbgb_params {
 /* Record per-target accepted-interaction counts (Barnes-Hut) or neighbour
  * counts (spatial hash) for nbgb_copy_interaction_counts(). */
 #define NBGB_FLAG_COUNT_INTERACTIONS 0x4u
+/* nbgb_system over a direct calculator: forces in FP64 from the FP64 state,
+ * accelerations kept in FP64 (the full-FP64 reference variant; FP64
+ * arithmetic runs at a small fraction of the FP32 rate on GB300). */
+#define NBGB_FLAG_FP64 0x8u
 
 void nbgb_params_default(nbgb_params* p);
 
@@ -221,7 +225,8 @@ nbgb_status nbgb_copy_interaction_counts(nbgb_calculator* calc, int32_t* counts,
  * Device-resident simulation with FP64 position/velocity state: the fast
  * path under ParticleSystem::update (src/core/particle_system.cpp:122-136).
  * Kick-drift-kick (algebraically the reference's Velocity Verlet,
- * src/cuda/integrator.cu:175-189) with x, v in FP64 and FP32 forces.
+ * src/cuda/integrator.cu:175-189) with x, v in FP64 and FP32 forces (FP64
+ * forces from the FP64 state when the calculator has NBGB_FLAG_FP64).
  * ------------------------------------------------------------------------- */
 typedef struct nbgb_system nbgb_system;
 
@@ -239,8 +244,9 @@ nbgb_status nbgb_system_read(nbgb_system* sys, nbgb_particle_data* h_out);
 /* FP64 state into host arrays (any pointer may be NULL). */
 nbgb_status nbgb_system_read_f64(nbgb_system* sys, double* x, double* y, double* z, double* vx,
                                  double* vy, double* vz);
-/* FP64 energy and momentum: KE = sum m v^2/2, PE = -sum_{i<j} G m_i m_j /
- * sqrt(r^2 + eps^2) (integrator.cu:52-120), P = sum m v. */
+/* FP64 energy and momentum from the FP64 state: KE = sum m v^2/2, PE =
+ * -sum_{i<j} G m_i m_j / sqrt(r^2 + eps^2) (integrator.cu:52-120; here in
+ * FP64 arithmetic, O(N^2)), P = sum m v. */
 nbgb_status nbgb_system_energy(nbgb_system* sys, double* ke, double* pe, double momentum[3]);
 
 /* ---------------------------------------------------------------------------
@@ -266,7 +272,8 @@ typedef struct nbgb_ensemble_config {
   float theta;               /* Barnes-Hut opening angle */
   int32_t leaf_capacity;     /* Barnes-Hut bucket size (1 = reference tree walk) */
   int32_t direct_config;     /* direct kernel configuration; -1 = autotune */
-  int32_t use_graphs;        /* capture each Barnes-Hut step as a CUDA graph */
+  int32_t use_graphs;        /* run the batched Barnes-Hut pass as a CUDA graph while the
+                                set of resident Barnes-Hut systems is unchanged */
 } nbgb_ensemble_config;
 
 /* One finished request. */
@@ -282,7 +289,7 @@ typedef struct nbgb_ensemble_stats {
   int64_t ticks;
   int64_t particle_steps;       /* sum over ticks of resident bodies */
   double direct_interactions;   /* sum of N (N - 1) over direct system-steps */
-  double bh_interactions;       /* accepted interactions (measured at admission) x steps */
+  double bh_interactions;       /* interactions summed by the Barnes-Hut walks (device count) */
   int64_t admitted;
   int64_t retired;
   int32_t resident;
@@ -306,9 +313,11 @@ nbgb_status nbgb_ensemble_submit(nbgb_ensemble* ens, const nbgb_particle_data* h
  * finished ones (their results become pollable when their copies land). */
 nbgb_status nbgb_ensemble_tick(nbgb_ensemble* ens, int32_t* resident, int32_t* queued);
 /* Pop one finished request.  Returns NBGB_ERR_NOT_READY when none is
- * available.  If h_out is non-NULL its pos/vel/acc/mass arrays (count
- * entries, host) receive the final FP32 state; state_f64 (6*count doubles
- * x, y, z, vx, vy, vz, or NULL) the FP64 state. */
+ * available.  If h_out is non-NULL and h_out->count (the capacity of its
+ * host arrays) is at least result->count, its non-NULL pos/vel/acc/mass
+ * arrays receive the final FP32 state (acc = the acceleration at the final
+ * positions); state_f64 (6*count doubles x, y, z, vx, vy, vz, or NULL) the
+ * FP64 state. */
 nbgb_status nbgb_ensemble_poll(nbgb_ensemble* ens, nbgb_ensemble_result* result,
                                nbgb_particle_data* h_out, double* state_f64);
 /* Wait for all retirements in flight. */

@@ -176,18 +176,36 @@ struct nbgb_system {
   int64_t n = 0;
   DevBuf<double> x, y, z, vx, vy, vz;
   DevBuf<float> ax, ay, az;
+  DevBuf<double> ax64, ay64, az64;  // NBGB_FLAG_FP64: accelerations in FP64
   DevBuf<float4> pm;
   DevBuf<double> red;
   HostPinned<double> h_red;
+  bool fp64 = false;
   bool pending_half = false;  // v lags x by half a kick of size last_dt/2
   double last_dt = 0.0;
 };
 
 static void system_sync_velocity(nbgb_system* s) {
   if (!s->pending_half) return;
-  launch_kick(s->n, s->vx.ptr, s->vy.ptr, s->vz.ptr, s->ax.ptr, s->ay.ptr, s->az.ptr,
-              0.5 * s->last_dt, s->calc->stream);
+  if (s->fp64)
+    launch_kick(s->n, s->vx.ptr, s->vy.ptr, s->vz.ptr, s->ax64.ptr, s->ay64.ptr, s->az64.ptr,
+                0.5 * s->last_dt, s->calc->stream);
+  else
+    launch_kick(s->n, s->vx.ptr, s->vy.ptr, s->vz.ptr, s->ax.ptr, s->ay.ptr, s->az.ptr,
+                0.5 * s->last_dt, s->calc->stream);
   s->pending_half = false;
+}
+
+// Forces at the current state into the system's acceleration arrays.
+static void system_forces(nbgb_system* s) {
+  nbgb_calculator* c = s->calc;
+  if (s->fp64) {
+    const double eps = (double)c->params.softening;
+    launch_direct_f64_state(s->x.ptr, s->y.ptr, s->z.ptr, s->pm.ptr, s->n, (double)c->params.G,
+                            eps * eps, s->ax64.ptr, s->ay64.ptr, s->az64.ptr, c->stream);
+  } else {
+    forces_packed(c, s->pm.ptr, s->n, s->ax.ptr, s->ay.ptr, s->az.ptr);
+  }
 }
 
 extern "C" {
@@ -468,6 +486,9 @@ nbgb_status nbgb_system_create(nbgb_calculator* calc, const nbgb_particle_data* 
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: null host array");
     auto s = std::make_unique<nbgb_system>();
     s->calc = calc;
+    s->fp64 = (calc->params.flags & NBGB_FLAG_FP64) != 0;
+    if (s->fp64 && calc->method != NBGB_DIRECT_N2)
+      fail(NBGB_ERR_INVALID_ARG, "Validation Error: FP64 forces require the direct method");
     const int64_t n = (int64_t)h->count;
     s->n = n;
     cudaStream_t st = calc->stream;
@@ -487,6 +508,11 @@ nbgb_status nbgb_system_create(nbgb_calculator* calc, const nbgb_particle_data* 
     s->ax.ensure((size_t)n);
     s->ay.ensure((size_t)n);
     s->az.ensure((size_t)n);
+    if (s->fp64) {
+      s->ax64.ensure((size_t)n);
+      s->ay64.ensure((size_t)n);
+      s->az64.ensure((size_t)n);
+    }
     const int64_t n_pad = direct_pad(n);
     float4* pm = s->pm.ensure((size_t)n_pad);
     std::vector<float4> hp((size_t)n_pad, make_float4(0.f, 0.f, 0.f, 0.f));
@@ -494,7 +520,7 @@ nbgb_status nbgb_system_create(nbgb_calculator* calc, const nbgb_particle_data* 
       hp[(size_t)i] = make_float4(h->pos_x[i], h->pos_y[i], h->pos_z[i], h->mass[i]);
     NBGB_CUDA(cudaMemcpyAsync(pm, hp.data(), (size_t)n_pad * sizeof(float4),
                               cudaMemcpyHostToDevice, st));
-    forces_packed(calc, pm, n, s->ax.ptr, s->ay.ptr, s->az.ptr);
+    system_forces(s.get());
     check_device_errors(calc);
     *out = s.release();
   });
@@ -519,9 +545,13 @@ nbgb_status nbgb_system_step(nbgb_system* s, float dt, int32_t steps) {
     const double h = (double)dt;
     for (int32_t k = 0; k < steps; ++k) {
       double kick = s->pending_half ? 0.5 * s->last_dt + 0.5 * h : 0.5 * h;
-      launch_kick_drift(s->n, s->x.ptr, s->y.ptr, s->z.ptr, s->vx.ptr, s->vy.ptr, s->vz.ptr,
-                        s->ax.ptr, s->ay.ptr, s->az.ptr, kick, h, s->pm.ptr, c->stream);
-      forces_packed(c, s->pm.ptr, s->n, s->ax.ptr, s->ay.ptr, s->az.ptr);
+      if (s->fp64)
+        launch_kick_drift(s->n, s->x.ptr, s->y.ptr, s->z.ptr, s->vx.ptr, s->vy.ptr, s->vz.ptr,
+                          s->ax64.ptr, s->ay64.ptr, s->az64.ptr, kick, h, s->pm.ptr, c->stream);
+      else
+        launch_kick_drift(s->n, s->x.ptr, s->y.ptr, s->z.ptr, s->vx.ptr, s->vy.ptr, s->vz.ptr,
+                          s->ax.ptr, s->ay.ptr, s->az.ptr, kick, h, s->pm.ptr, c->stream);
+      system_forces(s);
       s->pending_half = true;
       s->last_dt = h;
     }
@@ -552,9 +582,15 @@ nbgb_status nbgb_system_read(nbgb_system* s, nbgb_particle_data* h) {
     down(s->vx, h->vel_x);
     down(s->vy, h->vel_y);
     down(s->vz, h->vel_z);
-    if (h->acc_x) NBGB_CUDA(cudaMemcpyAsync(h->acc_x, s->ax.ptr, n * 4, cudaMemcpyDeviceToHost, st));
-    if (h->acc_y) NBGB_CUDA(cudaMemcpyAsync(h->acc_y, s->ay.ptr, n * 4, cudaMemcpyDeviceToHost, st));
-    if (h->acc_z) NBGB_CUDA(cudaMemcpyAsync(h->acc_z, s->az.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+    if (s->fp64) {
+      down(s->ax64, h->acc_x);
+      down(s->ay64, h->acc_y);
+      down(s->az64, h->acc_z);
+    } else {
+      if (h->acc_x) NBGB_CUDA(cudaMemcpyAsync(h->acc_x, s->ax.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+      if (h->acc_y) NBGB_CUDA(cudaMemcpyAsync(h->acc_y, s->ay.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+      if (h->acc_z) NBGB_CUDA(cudaMemcpyAsync(h->acc_z, s->az.ptr, n * 4, cudaMemcpyDeviceToHost, st));
+    }
     if (h->mass) {
       std::vector<float4> hp(n);
       NBGB_CUDA(cudaMemcpyAsync(hp.data(), s->pm.ptr, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
@@ -597,8 +633,10 @@ nbgb_status nbgb_system_energy(nbgb_system* s, double* ke, double* pe, double mo
     double kin[4] = {h[0], h[1], h[2], h[3]};
     double pot = 0.0;
     if (pe) {
-      const float eps = c->params.softening;
-      launch_potential(s->pm.ptr, s->n, eps * eps, p, nb, p + (size_t)nb * 4, st);
+      // FP64 positions, FP64 arithmetic (the state the system integrates)
+      const double eps = (double)c->params.softening;
+      launch_potential_f64(s->x.ptr, s->y.ptr, s->z.ptr, s->pm.ptr, s->n, eps * eps, p, nb,
+                           p + (size_t)nb * 4, st);
       NBGB_CUDA(cudaMemcpyAsync(h, p + (size_t)nb * 4, sizeof(double), cudaMemcpyDeviceToHost, st));
       NBGB_CUDA(cudaStreamSynchronize(st));
       pot = (double)c->params.G * h[0];

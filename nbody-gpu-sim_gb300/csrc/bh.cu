@@ -1,5 +1,6 @@
-// bh.cu -- Barnes-Hut on the device: Morton keys, radix sort, octree from
-// sorted path keys, bottom-up centre of mass, warp-cooperative walk (K2-K6).
+// bh.cu -- Barnes-Hut on the device: path keys, radix sort, octree from
+// sorted keys, bottom-up centre of mass, warp-cooperative walk (K2-K6), for
+// one system or for many independent systems ("segments") in one pass.
 //
 // Replaces BarnesHutTree::build/computeForces and BarnesHutCalculator
 // (src/cuda/force_barnes_hut.cu:125-583), whose octree is built on the host
@@ -12,25 +13,29 @@
 // node-budget merge (:449-453, which only fires for N below ~64) that tree
 // is canonical: a node exists for every octant-path prefix whose parent holds
 // >= 2 bodies, a leaf is the shortest prefix unique to its body, and depth-32
-// cells hold all their bodies.  This file builds exactly that tree in
-// parallel:
-//   1. path key of every body: its 32 octants, computed with the
-//      reference's float operations from the reference's root cube;
-//   2. stable radix sort by path key (ties keep Morton order = the
-//      reference's insertion order, which fixes merged-leaf sums);
-//   3. l_k = common levels of adjacent sorted keys; body k starts the
-//      internal nodes of depths l_{k-1}+1 .. min(l_k, 31) and (unless it
-//      shares a depth-32 cell with k-1) one leaf of depth
-//      min(32, max(l_{k-1}, l_k) + 1);
+// cells hold all their bodies.  It is built here in parallel:
+//   1. per segment, the bounding box and the reference's root cube; every
+//      body's path key = its 32 octants, computed with the reference's float
+//      operations (levels 1..21 in a high 63-bit key, 22..32 in a low key);
+//   2. stable radix sort by the high key, then (several segments) by
+//      segment; bodies sharing segment and high key are put in (low key,
+//      Morton key, index) order, i.e. the reference's insertion order inside
+//      a shared depth-32 cell;
+//   3. l_k = common levels of adjacent sorted keys of one segment; body k
+//      starts the internal nodes of depths l_{k-1}+1 .. min(l_k, 31) and
+//      (unless it shares a depth-32 cell with k-1) one leaf of depth
+//      min(32, max(l_{k-1}, l_k) + 1); the first body of a segment also
+//      starts the segment's root;
 //   4. an exclusive scan of those counts numbers the nodes in depth-first
-//      pre-order (children in octant order), so every subtree is a
-//      contiguous index range and skip(P) = first node of body end(P)+1;
+//      pre-order (children in octant order): every subtree, and every
+//      segment's tree, is a contiguous index range, and
+//      skip(P) = first node of body end(P)+1;
 //   5. centres of mass bottom-up with per-node arrival counters, summing
 //      children in octant order with the reference's float operations
 //      (:514-538), so masses and centres of mass are bit-identical.
 //
-// Walk.  One warp walks the pre-order array for 32 consecutive targets
-// (Morton/path-sorted, so spatially close).  Every lane applies the
+// Walk.  One warp walks its segment's pre-order range for 32 consecutive
+// targets (path-sorted, so spatially close).  Every lane applies the
 // reference's per-target rules (contains_i, leaf self-subtraction, opening
 // test 4h^2/(d^2+eps^2) < theta^2, :175-243); the warp descends into a node
 // if any active lane opens it, and a lane that accepted a node sleeps until
@@ -38,6 +43,10 @@
 // the reference's interaction set for its target (no stack, no local
 // memory, broadcast node loads).  With leaf_capacity > 1 a subtree holding
 // at most that many bodies is summed body by body when opened.
+#include <algorithm>
+#include <vector>
+
+#include "bh.cuh"
 #include "common.cuh"
 #include "geom.cuh"
 #include "kernels.cuh"
@@ -51,27 +60,40 @@ constexpr int kHiLevels = 21;  // levels 1..21 in the high key (63 bits)
 constexpr int kMaxDepth = 32;  // force_barnes_hut.cu:24
 
 struct BHState {
-  DevBuf<float> bbox_part;
-  DevBuf<BBox> box;
-  DevBuf<uint32_t> mkeys, mkeys_alt, midx, midx_alt;  // Morton sort
-  DevBuf<u64> klo, klo_alt, khi, khi_alt;             // path keys
-  DevBuf<uint32_t> pidx, pidx_alt;
+  // segment tables (device; single-system calls fill one segment)
+  DevBuf<char> tables;           // seg_off [nseg], seg_base [nseg + 1], tasks [ntasks]
+  int64_t* seg_off_p = nullptr;
+  int64_t* seg_base_p = nullptr;
+  WarpTask* tasks_p = nullptr;
+  DevBuf<int32_t> seg_of;
+  DevBuf<uint32_t> seg_minmax;   // [6][nseg] ordered-uint encoded bounds
+  DevBuf<BBox> box;              // [nseg]
+  DevBuf<int32_t> seg_root, seg_end, seg_depth;  // per segment
+  HostPinned<char> h_tables;
+  int32_t nseg = 0;
+  int64_t ntasks = 0;
+  // keys and order
+  DevBuf<uint32_t> mkeys, mkeys_alt, midx, midx_alt;  // on-demand Morton sort
+  DevBuf<u64> klo, khi, khi_alt;
+  DevBuf<uint32_t> pidx, pidx_alt, sk, sk_alt;
+  DevBuf<int32_t> kseg;          // segment of sorted position k
   DevBuf<uint32_t> hist, scan_ws;
   DevBuf<uint8_t> lcp;
   DevBuf<uint32_t> ncnt;    // n + 1
   DevBuf<uint32_t> nstart;  // n + 1
-  DevBuf<uint32_t> scalars; // [0] total nodes, [1] max depth
+  DevBuf<uint32_t> scalars; // [0] total nodes
   HostPinned<uint32_t> h_scalars;
   DevBuf<float4> node_com, node_geom;
   DevBuf<int4> node_info;  // skip, first, count, flags (bit0 leaf, bits 8.. depth)
   DevBuf<int32_t> node_parent, node_nchild, node_visit;
   DevBuf<float4> spm;      // bodies in path order
+  DevBuf<unsigned long long> inter_total;
   int64_t n = 0;
-  int64_t cap = 0;
-  bool m_alt = false;      // Morton result in *_alt
-  bool keys_valid = false; // Morton (key, index) pairs computed for the last build
-  const uint32_t* body = nullptr;  // path-sorted body indices
-  const u64* hi_sorted = nullptr;
+  int64_t reserve = 0;  // bodies the per-body buffers are sized for (>= n)
+  int64_t cap = 0;      // node capacity
+  bool m_alt = false;       // Morton result in *_alt
+  bool keys_valid = false;  // Morton (key, index) pairs computed for the last build
+  const uint32_t* body = nullptr;  // path-sorted concatenated body indices
 };
 
 void bh_state_delete(BHState* p) { delete p; }
@@ -97,19 +119,9 @@ __device__ __forceinline__ uint32_t morton_of(float4 p, const BBox& b) {
   return (spread3(ix) << 2) | (spread3(iy) << 1) | spread3(iz);
 }
 
-__global__ void morton_kernel(const float4* __restrict__ pm, int64_t n, const BBox* __restrict__ box,
-                              uint32_t* __restrict__ keys, uint32_t* __restrict__ idx) {
-  const BBox b = *box;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    keys[i] = morton_of(pm[i], b);
-    idx[i] = (uint32_t)i;
-  }
-}
-
-// Octant path of a position through the reference's subdivision: returns the
-// high key (levels 1..21, 3 bits each, level 1 most significant) and the low
-// key (levels 22..32).
+// Octant path of a position through the reference's subdivision: the high
+// key (levels 1..21, 3 bits each, level 1 most significant) and the low key
+// (levels 22..32).
 __device__ __forceinline__ void path_key(float4 p, const BBox& b, u64& hi, u64& lo) {
   float cx = b.center[0], cy = b.center[1], cz = b.center[2], h = b.half;
   u64 a = 0, c = 0;
@@ -130,80 +142,178 @@ __device__ __forceinline__ void path_key(float4 p, const BBox& b, u64& hi, u64& 
   lo = c;
 }
 
-// Centre and half size of the depth-d cell on a body's path.
-__device__ __forceinline__ float4 cell_at_depth(float4 p, const BBox& b, int d) {
-  float cx = b.center[0], cy = b.center[1], cz = b.center[2], h = b.half;
-  for (int lev = 1; lev <= d; ++lev) {
-    const uint32_t o = (p.x >= cx ? 1u : 0u) | (p.y >= cy ? 2u : 0u) | (p.z >= cz ? 4u : 0u);
-    const float hs = __fmul_rn(h, 0.5f);
-    cx = __fadd_rn(cx, (o & 1u) ? hs : -hs);
-    cy = __fadd_rn(cy, (o & 2u) ? hs : -hs);
-    cz = __fadd_rn(cz, (o & 4u) ? hs : -hs);
-    h = hs;
+struct SegView {
+  const int64_t* off;   // arena offset of segment s
+  const int64_t* base;  // first concatenated index of segment s (nseg + 1 entries)
+  const int32_t* seg_of;
+  const BBox* box;
+  __device__ __forceinline__ int64_t arena(uint32_t q) const {
+    const int s = seg_of[q];
+    return off[s] + ((int64_t)q - base[s]);
   }
-  return make_float4(cx, cy, cz, h);
+};
+
+// ----------------------------------------------------- segment setup --
+__global__ void seg_of_kernel(const int64_t* __restrict__ base, int nseg, int64_t n,
+                              int32_t* __restrict__ seg_of) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {  // last s with base[s] <= q
+      const int mid = (lo + hi + 1) >> 1;
+      if (base[mid] <= q)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    seg_of[q] = lo;
+  }
 }
 
-// After the Morton sort: low path keys in Morton order (values = bodies).
-__global__ void path_lo_kernel(const float4* __restrict__ pm, const uint32_t* __restrict__ body,
-                               int64_t n, const BBox* __restrict__ box, u64* __restrict__ lo,
-                               uint32_t* __restrict__ out_body) {
-  const BBox b = *box;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t i = body[k];
-    u64 h, l;
-    path_key(pm[i], b, h, l);
-    lo[k] = l;
-    out_body[k] = i;
+// Order-preserving float <-> uint32 (for exact min/max with integer atomics).
+__device__ __forceinline__ uint32_t f2ord(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float ord2f(uint32_t u) {
+  return __uint_as_float((u & 0x80000000u) ? (u & 0x7fffffffu) : ~u);
+}
+
+// Per-segment min/max of the bodies.  A block reduces a contiguous chunk;
+// when the chunk lies in one segment (the common case) it issues one atomic
+// per bound, otherwise each warp (or lane) does.  Min/max are exact, so the
+// result equals the reference's computeBoundingBoxKernel (:78-122).
+__global__ void seg_bounds_kernel(const float4* __restrict__ pm, SegView sv, int64_t n, int nseg,
+                                  uint32_t* __restrict__ mm) {
+  __shared__ float s_red[32][6];
+  __shared__ int s_same;
+  const int64_t c0 = (int64_t)blockIdx.x * blockDim.x * 4;
+  const int64_t c1 = imin64(c0 + (int64_t)blockDim.x * 4, n);
+  if (c0 >= n) return;
+  if (threadIdx.x == 0) s_same = (sv.seg_of[c0] == sv.seg_of[c1 - 1]);
+  __syncthreads();
+  const bool same = s_same;
+  float v[6] = {1e30f, 1e30f, 1e30f, -1e30f, -1e30f, -1e30f};
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = 0; r < 4; ++r) {
+    const int64_t q = c0 + (int64_t)r * blockDim.x + threadIdx.x;
+    if (q < c1) {
+      const float4 p = pm[sv.arena((uint32_t)q)];
+      if (same) {
+        v[0] = fminf(v[0], p.x);
+        v[1] = fminf(v[1], p.y);
+        v[2] = fminf(v[2], p.z);
+        v[3] = fmaxf(v[3], p.x);
+        v[4] = fmaxf(v[4], p.y);
+        v[5] = fmaxf(v[5], p.z);
+      } else {
+        const int s = sv.seg_of[q];
+        atomicMin(&mm[0 * nseg + s], f2ord(p.x));
+        atomicMin(&mm[1 * nseg + s], f2ord(p.y));
+        atomicMin(&mm[2 * nseg + s], f2ord(p.z));
+        atomicMax(&mm[3 * nseg + s], f2ord(p.x));
+        atomicMax(&mm[4 * nseg + s], f2ord(p.y));
+        atomicMax(&mm[5 * nseg + s], f2ord(p.z));
+      }
+    }
+  }
+  if (!same) return;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      v[a] = fminf(v[a], __shfl_down_sync(0xffffffffu, v[a], o));
+      v[3 + a] = fmaxf(v[3 + a], __shfl_down_sync(0xffffffffu, v[3 + a], o));
+    }
+  if (lane == 0)
+    for (int a = 0; a < 6; ++a) s_red[warp][a] = v[a];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w)
+      for (int a = 0; a < 3; ++a) {
+        v[a] = fminf(v[a], s_red[w][a]);
+        v[3 + a] = fmaxf(v[3 + a], s_red[w][3 + a]);
+      }
+    const int s = sv.seg_of[c0];
+    for (int a = 0; a < 3; ++a) {
+      atomicMin(&mm[a * nseg + s], f2ord(v[a]));
+      atomicMax(&mm[(3 + a) * nseg + s], f2ord(v[3 + a]));
+    }
   }
 }
 
-__global__ void path_hi_kernel(const float4* __restrict__ pm, const uint32_t* __restrict__ body,
-                               int64_t n, const BBox* __restrict__ box, u64* __restrict__ hi) {
-  const BBox b = *box;
+// Per segment: the reference's derived constants with its float operations
+//   Morton scale  inv = 1.0f / (max - min + 0.001f)            (:313-320)
+//   root centre   (min + max) * 0.5f                           (:418-419)
+//   root half     max(ex, ey, ez) * 0.5f + 0.001f, first max   (:420-422)
+__global__ void seg_box_kernel(const uint32_t* __restrict__ mm, int nseg, BBox* __restrict__ box,
+                               uint32_t* err) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < nseg; s += gridDim.x * blockDim.x) {
+    BBox o;
+    bool ok = true;
+    for (int a = 0; a < 3; ++a) {
+      const float mn = ord2f(mm[a * nseg + s]), mx = ord2f(mm[(3 + a) * nseg + s]);
+      o.min[a] = mn;
+      o.max[a] = mx;
+      ok = ok && isfinite(mn) && isfinite(mx);
+      o.inv[a] = __fdiv_rn(1.0f, __fadd_rn(__fsub_rn(mx, mn), 0.001f));
+      o.center[a] = __fmul_rn(__fadd_rn(mn, mx), 0.5f);
+    }
+    const float ex = __fsub_rn(o.max[0], o.min[0]), ey = __fsub_rn(o.max[1], o.min[1]),
+                ez = __fsub_rn(o.max[2], o.min[2]);
+    float ms = ex;
+    if (ms < ey) ms = ey;
+    if (ms < ez) ms = ez;
+    o.half = __fadd_rn(__fmul_rn(ms, 0.5f), 0.001f);
+    o.valid = ok ? 1 : 0;
+    if (!ok) raise_error(err, kErrBadInput);
+    box[s] = o;
+  }
+}
+
+// High path key of every body in concatenated order (values = indices).
+__global__ void path_hi_index_kernel(const float4* __restrict__ pm, SegView sv, int64_t n,
+                                     u64* __restrict__ hi, uint32_t* __restrict__ idx) {
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    u64 h, l;
+    path_key(pm[sv.arena((uint32_t)q)], sv.box[sv.seg_of[q]], h, l);
+    hi[q] = h;
+    idx[q] = (uint32_t)q;
+  }
+}
+
+__global__ void seg_key_kernel(const uint32_t* __restrict__ idx, const int32_t* __restrict__ seg_of,
+                               int64_t n, uint32_t* __restrict__ sk) {
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x)
+    sk[k] = (uint32_t)seg_of[idx[k]];
+}
+
+// Final order: segment, both path keys and the body itself per position.
+__global__ void path_final_kernel(const float4* __restrict__ pm, SegView sv,
+                                  const uint32_t* __restrict__ body, int64_t n,
+                                  int32_t* __restrict__ kseg, u64* __restrict__ hi,
+                                  u64* __restrict__ lo, float4* __restrict__ spm) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t q = body[k];
+    const int s = sv.seg_of[q];
+    const float4 p = pm[sv.off[s] + ((int64_t)q - sv.base[s])];
     u64 h, l;
-    path_key(pm[body[k]], b, h, l);
+    path_key(p, sv.box[s], h, l);
+    kseg[k] = s;
     hi[k] = h;
-  }
-}
-
-// Final order: low keys recomputed in path order, bodies gathered (x,y,z,m).
-__global__ void path_final_kernel(const float4* __restrict__ pm, const uint32_t* __restrict__ body,
-                                  int64_t n, const BBox* __restrict__ box, u64* __restrict__ lo,
-                                  float4* __restrict__ spm) {
-  const BBox b = *box;
-  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-       k += (int64_t)gridDim.x * blockDim.x) {
-    const float4 p = pm[body[k]];
-    u64 h, l;
-    path_key(p, b, h, l);
     lo[k] = l;
     spm[k] = p;
   }
 }
 
-// High path key of every body in index order (values = body indices).
-__global__ void path_hi_index_kernel(const float4* __restrict__ pm, int64_t n,
-                                     const BBox* __restrict__ box, u64* __restrict__ hi,
-                                     uint32_t* __restrict__ idx) {
-  const BBox b = *box;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x) {
-    u64 h, l;
-    path_key(pm[i], b, h, l);
-    hi[i] = h;
-    idx[i] = (uint32_t)i;
-  }
-}
-
-// Tie key of a body: low path key, then Morton key, then index.
-__device__ __forceinline__ bool tie_less(const float4* __restrict__ pm, const BBox& b, uint32_t a,
-                                         uint32_t c) {
+// Tie key inside a run of equal (segment, high key): low key, then Morton
+// key, then index.
+__device__ __forceinline__ bool tie_less(const float4& pa, uint32_t a, const float4& pc,
+                                         uint32_t c, const BBox& b) {
   u64 ha, la, hc, lc;
-  const float4 pa = pm[a], pc = pm[c];
   path_key(pa, b, ha, la);
   path_key(pc, b, hc, lc);
   if (la != lc) return la < lc;
@@ -212,33 +322,46 @@ __device__ __forceinline__ bool tie_less(const float4* __restrict__ pm, const BB
   return a < c;
 }
 
-// Runs of equal high keys (bodies sharing their first 21 octants; tiny in
-// practice) are put in (low key, Morton key, index) order by one thread per
-// run with an insertion sort.  A run that is already in order (e.g. many
-// coincident bodies) costs one comparison per body.
-__global__ void tie_order_kernel(const float4* __restrict__ pm, int64_t n,
-                                 const BBox* __restrict__ box, const u64* __restrict__ hi,
-                                 uint32_t* __restrict__ body) {
-  const BBox b = *box;
+// Runs of equal (segment, high key) -- bodies sharing their first 21
+// octants, tiny in practice -- are insertion-sorted by one thread per run;
+// positions of a run that moved get their body, low key and payload fixed.
+// A run already in order (e.g. coincident bodies) costs one comparison per
+// body.
+__global__ void tie_order_kernel(SegView sv, int64_t n, const int32_t* __restrict__ kseg,
+                                 const u64* __restrict__ hi, uint32_t* __restrict__ body,
+                                 u64* __restrict__ lo, float4* __restrict__ spm) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k + 1 < n;
        k += (int64_t)gridDim.x * blockDim.x) {
-    if (k > 0 && hi[k - 1] == hi[k]) continue;  // not the start of a run
-    if (hi[k + 1] != hi[k]) continue;           // run of one
+    if (k > 0 && hi[k - 1] == hi[k] && kseg[k - 1] == kseg[k]) continue;
+    if (hi[k + 1] != hi[k] || kseg[k + 1] != kseg[k]) continue;
     int64_t e = k + 1;
-    while (e + 1 < n && hi[e + 1] == hi[k]) ++e;
+    while (e + 1 < n && hi[e + 1] == hi[k] && kseg[e + 1] == kseg[k]) ++e;
+    const BBox b = sv.box[kseg[k]];
+    bool moved = false;
     for (int64_t i = k + 1; i <= e; ++i) {
       const uint32_t cur = body[i];
+      const float4 pc = spm[i];
       int64_t j = i - 1;
-      while (j >= k && tie_less(pm, b, cur, body[j])) {
+      while (j >= k && tie_less(pc, cur, spm[j], body[j], b)) {
         body[j + 1] = body[j];
+        spm[j + 1] = spm[j];
         --j;
+        moved = true;
       }
       body[j + 1] = cur;
+      spm[j + 1] = pc;
     }
+    if (moved)
+      for (int64_t i = k; i <= e; ++i) {
+        u64 h, l;
+        path_key(spm[i], b, h, l);
+        lo[i] = l;
+      }
   }
 }
 
-// Morton keys scattered back to index order (for the on-demand key sort).
+// Morton keys scattered back to index order (for the on-demand key sort of a
+// single system).
 __global__ void morton_scatter_kernel(const float4* __restrict__ spm,
                                       const uint32_t* __restrict__ body, int64_t n,
                                       const BBox* __restrict__ box, uint32_t* __restrict__ keys,
@@ -258,40 +381,52 @@ __device__ __forceinline__ int common_levels(u64 h0, u64 l0, u64 h1, u64 l1) {
   return kMaxDepth;
 }
 
-// l_k for k in [0, n-1); per-body node counts (internal + leaf, + root at 0).
-__global__ void lcp_count_kernel(const u64* __restrict__ hi, const u64* __restrict__ lo, int64_t n,
-                                 uint8_t* __restrict__ lcp, uint32_t* __restrict__ cnt) {
+// l_k (0 across a segment boundary) and per-body node counts: internal +
+// leaf, + the root at the first body of a segment.
+__global__ void lcp_count_kernel(const int32_t* __restrict__ kseg, const u64* __restrict__ hi,
+                                 const u64* __restrict__ lo, int64_t n, uint8_t* __restrict__ lcp,
+                                 uint32_t* __restrict__ cnt) {
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
-    const int lk = (k + 1 < n) ? common_levels(hi[k], lo[k], hi[k + 1], lo[k + 1]) : 0;
-    const int lp = (k > 0) ? common_levels(hi[k - 1], lo[k - 1], hi[k], lo[k]) : 0;
+    const bool first = (k == 0) || kseg[k - 1] != kseg[k];
+    const bool last = (k + 1 == n) || kseg[k + 1] != kseg[k];
+    const int lk = last ? 0 : common_levels(hi[k], lo[k], hi[k + 1], lo[k + 1]);
+    const int lp = first ? 0 : common_levels(hi[k - 1], lo[k - 1], hi[k], lo[k]);
     if (k + 1 < n) lcp[k] = (uint8_t)lk;
-    const int fd = (k > 0) ? lp + 1 : 1;
-    const int top = (k + 1 < n) ? min(lk, kMaxDepth - 1) : 0;
+    const int fd = first ? 1 : lp + 1;
+    const int top = last ? 0 : min(lk, kMaxDepth - 1);
     uint32_t c = (uint32_t)max(0, top - fd + 1);
-    const bool leaf_start = (k == 0) || (lp < kMaxDepth);
+    const bool leaf_start = first || (lp < kMaxDepth);
     c += leaf_start ? 1u : 0u;
-    if (k == 0) c += 1u;  // root
+    if (first) c += 1u;  // the segment's root
     cnt[k] = c;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) cnt[n] = 0;
 }
 
-// Range end of the depth-d node that contains sorted body k: the largest j
-// with common_levels(key_k, key_j) >= d.  Keys are sorted, so that predicate
-// is monotone in j: gallop, then bisect (Karras-style, O(log range)).
-__device__ __forceinline__ int64_t range_end(const u64* __restrict__ hi, const u64* __restrict__ lo,
+// Range end of the depth-d node that contains sorted body k: the largest j of
+// the same segment with common_levels(key_k, key_j) >= d.  Keys are sorted
+// and segments contiguous, so the predicate is monotone in j: gallop, then
+// bisect (Karras-style, O(log range)).
+__device__ __forceinline__ bool same_prefix(const int32_t* kseg, const u64* hi, const u64* lo,
+                                            int32_t s0, u64 h0, u64 l0, int64_t j, int d) {
+  return kseg[j] == s0 && common_levels(h0, l0, hi[j], lo[j]) >= d;
+}
+
+__device__ __forceinline__ int64_t range_end(const int32_t* __restrict__ kseg,
+                                             const u64* __restrict__ hi, const u64* __restrict__ lo,
                                              int64_t n, int64_t k, int d) {
   const u64 h0 = hi[k], l0 = lo[k];
+  const int32_t s0 = kseg[k];
   int64_t good = k, step = 1;
-  while (k + step < n && common_levels(h0, l0, hi[k + step], lo[k + step]) >= d) {
+  while (k + step < n && same_prefix(kseg, hi, lo, s0, h0, l0, k + step, d)) {
     good = k + step;
     step <<= 1;
   }
   int64_t bad = (k + step < n) ? k + step : n;
   while (bad - good > 1) {
     const int64_t mid = good + ((bad - good) >> 1);
-    if (common_levels(h0, l0, hi[mid], lo[mid]) >= d)
+    if (same_prefix(kseg, hi, lo, s0, h0, l0, mid, d))
       good = mid;
     else
       bad = mid;
@@ -300,19 +435,23 @@ __device__ __forceinline__ int64_t range_end(const u64* __restrict__ hi, const u
 }
 
 struct EmitArgs {
+  const int32_t* kseg;
   const uint8_t* lcp;
   const u64* hi;
   const u64* lo;
   const uint32_t* nstart;
-  const uint32_t* body;
   const float4* spm;
   const BBox* box;
+  const int64_t* base;  // segment s occupies sorted positions [base[s], base[s+1])
   int64_t n;
   int64_t cap;
   float4* geom;
   int4* info;
+  int32_t* parent;
   int32_t* visit;
-  uint32_t* scalars;
+  int32_t* seg_root;
+  int32_t* seg_end;
+  int32_t* seg_depth;
   uint32_t* err;
 };
 
@@ -322,27 +461,35 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
     if (blockIdx.x == 0 && threadIdx.x == 0) raise_error(a.err, kErrTreeCapacity);
     return;
   }
-  const BBox b = *a.box;
   for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < a.n;
        k += (int64_t)gridDim.x * blockDim.x) {
-    const int lk = (k + 1 < a.n) ? (int)a.lcp[k] : 0;
-    const int lp = (k > 0) ? (int)a.lcp[k - 1] : 0;
-    const int fd = (k > 0) ? lp + 1 : 1;
-    const int top = (k + 1 < a.n) ? min(lk, kMaxDepth - 1) : 0;
+    const int32_t s = a.kseg[k];
+    const bool first = (k == 0) || a.kseg[k - 1] != s;
+    const bool last = (k + 1 == a.n) || a.kseg[k + 1] != s;
+    const int lk = last ? 0 : (int)a.lcp[k];
+    const int lp = first ? 0 : (int)a.lcp[k - 1];
+    const int fd = first ? 1 : lp + 1;
+    const int top = last ? 0 : min(lk, kMaxDepth - 1);
     uint32_t idx = a.nstart[k];
     const float4 p = a.spm[k];
-    if (k == 0) {
-      a.geom[0] = make_float4(b.center[0], b.center[1], b.center[2], b.half);
-      a.info[0] = make_int4((int)total, 0, (int)a.n, 0);
-      a.visit[0] = 0;
+    const BBox b = a.box[s];
+    if (first) {
+      const int64_t send = a.base[s + 1];  // one past the segment's last position
+      const uint32_t skip = (send < a.n) ? a.nstart[send] : total;
+      a.geom[idx] = make_float4(b.center[0], b.center[1], b.center[2], b.half);
+      a.info[idx] = make_int4((int)skip, (int)k, (int)(send - k), 0);
+      a.parent[idx] = -1;
+      a.visit[idx] = 0;
+      a.seg_root[s] = (int32_t)idx;
+      a.seg_end[s] = (int32_t)skip;
       ++idx;
     }
     // walk the path of body k once, emitting internal nodes of depth fd..top
     float cx = b.center[0], cy = b.center[1], cz = b.center[2], h = b.half;
-    const bool leaf_start = (k == 0) || (lp < kMaxDepth);
+    const bool leaf_start = first || (lp < kMaxDepth);
     const int ld = min(kMaxDepth, max(lp, lk) + 1);
-    const int last = leaf_start ? ld : top;
-    for (int lev = 1; lev <= last; ++lev) {
+    const int lastlev = leaf_start ? ld : top;
+    for (int lev = 1; lev <= lastlev; ++lev) {
       const uint32_t o = (p.x >= cx ? 1u : 0u) | (p.y >= cy ? 2u : 0u) | (p.z >= cz ? 4u : 0u);
       const float hs = __fmul_rn(h, 0.5f);
       cx = __fadd_rn(cx, (o & 1u) ? hs : -hs);
@@ -350,7 +497,7 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
       cz = __fadd_rn(cz, (o & 4u) ? hs : -hs);
       h = hs;
       if (lev >= fd && lev <= top) {
-        const int64_t e = range_end(a.hi, a.lo, a.n, k, lev);
+        const int64_t e = range_end(a.kseg, a.hi, a.lo, a.n, k, lev);
         const uint32_t skip = (e + 1 < a.n) ? a.nstart[e + 1] : total;
         a.geom[idx] = make_float4(cx, cy, cz, h);
         a.info[idx] = make_int4((int)skip, (int)k, (int)(e - k + 1), lev << 8);
@@ -360,13 +507,13 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
     }
     if (leaf_start) {
       int64_t e = k;
-      while (e + 1 < a.n && (int)a.lcp[e] >= kMaxDepth) ++e;  // bodies sharing a depth-32 cell
+      while (e + 1 < a.n && a.kseg[e + 1] == s && (int)a.lcp[e] >= kMaxDepth) ++e;
       a.geom[idx] = make_float4(cx, cy, cz, h);
       a.info[idx] = make_int4((int)(idx + 1), (int)k, (int)(e - k + 1), (ld << 8) | 1);
       a.visit[idx] = 0;
       // reference max_depth_: depth of the inserting body's last loop level
       const int md = (ld == kMaxDepth && e > k) ? kMaxDepth : ld - 1;
-      atomicMax(&a.scalars[1], (uint32_t)md);
+      atomicMax(&a.seg_depth[s], md);
     }
   }
 }
@@ -380,7 +527,6 @@ __global__ void link_kernel(const int4* __restrict__ info, const uint32_t* __res
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
        p += (int64_t)gridDim.x * blockDim.x) {
     const int4 ip = info[p];
-    if (p == 0) parent[0] = -1;
     if (ip.w & 1) {
       nchild[p] = 0;
       continue;
@@ -456,6 +602,11 @@ struct WalkArgs {
   const float4* spm;
   const uint32_t* body;
   const uint32_t* nstart;
+  SegView sv;
+  const WarpTask* tasks;
+  int64_t ntasks;
+  const int32_t* seg_root;
+  const int32_t* seg_end;
   int64_t n;
   int64_t cap;
   float theta2;
@@ -465,7 +616,8 @@ struct WalkArgs {
   float* ax;
   float* ay;
   float* az;
-  int32_t* counts;
+  int32_t* counts;                  // per-body interaction counts (or null)
+  unsigned long long* inter_total;  // sum of interactions (or null)
 };
 
 // The reference's opening test `size2 / dist2 < theta2` with the correctly
@@ -493,15 +645,24 @@ __device__ __forceinline__ void bh_add(float px, float py, float pz, float m, fl
   sz = fmaf(f, dz, sz);
 }
 
-// One warp, 32 targets, each lane applying the reference's per-target rules
-// (union traversal; see the file header).  Adds into sx/sy/sz/cnt.
 template <bool COUNT, bool BUCKET>
-__device__ __forceinline__ void lane_walk(const WalkArgs& a, int64_t k, bool valid, float4 pi,
-                                          uint32_t total, bool tree_ok, float& sx, float& sy,
-                                          float& sz, int& cnt) {
+__global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
+  const uint32_t total = a.nstart[a.n];
+  const bool tree_ok = (int64_t)total <= a.cap;
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < a.ntasks;
+       t += warps) {
+    const WarpTask task = a.tasks[t];
+    const int64_t k = task.first + lane;
+    const bool valid = k < task.end;
+    const float4 pi = valid ? a.spm[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    int cnt = 0;
     int resume = valid ? 0 : 0x7fffffff;
-    int node = tree_ok ? 0 : (int)total;
-    while (node < (int)total) {
+    int node = tree_ok ? a.seg_root[task.seg] : 0;
+    const int node_end = tree_ok ? a.seg_end[task.seg] : 0;
+    while (node < node_end) {
       const float4 cm = a.com[node];
       const int4 in = a.info[node];
       if (cm.w == 0.0f) {  // force_barnes_hut.cu:172-173
@@ -564,28 +725,18 @@ __device__ __forceinline__ void lane_walk(const WalkArgs& a, int64_t k, bool val
       }
       node = __any_sync(0xffffffffu, open) ? node + 1 : in.x;
     }
-}
-
-template <bool COUNT, bool BUCKET>
-__global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
-  const uint32_t total = a.nstart[a.n];
-  const bool tree_ok = (int64_t)total <= a.cap;
-  const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t wbase = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; wbase < a.n;
-       wbase += warps * 32) {
-    const int64_t k = wbase + lane;
-    const bool valid = k < a.n;
-    const float4 pi = valid ? a.spm[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    int cnt = 0;
-    lane_walk<COUNT, BUCKET>(a, k, valid, pi, total, tree_ok, sx, sy, sz, cnt);
     if (valid) {
-      const uint32_t i = a.body[k];
+      const int64_t i = a.sv.arena(a.body[k]);
       a.ax[i] = a.G * sx;
       a.ay[i] = a.G * sy;
       a.az[i] = a.G * sz;
-      if (COUNT) a.counts[i] = cnt;
+      if (COUNT && a.counts) a.counts[i] = cnt;
+    }
+    if (COUNT && a.inter_total) {
+      unsigned long long c = valid ? (unsigned long long)cnt : 0ull;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+      if (lane == 0) atomicAdd(a.inter_total, c);
     }
   }
 }
@@ -595,57 +746,146 @@ static unsigned grid1d(int64_t n, int threads = 256) {
       1, std::min<int64_t>(ceil_div(std::max<int64_t>(n, 1), threads), (int64_t)num_sms() * 32));
 }
 
-// Builds the tree for n packed bodies; returns false if the node capacity
-// was too small (the needed count is then in h.h_scalars after a sync).
-static void bh_build(nbgb_calculator* c, BHState& h, const float4* pm, int64_t n) {
-  cudaStream_t st = c->stream;
-  uint32_t* err = c->err.ensure(1);
+// ------------------------------------------------------ host driver --
+size_t bh_state_bytes(const BHState* p) {
+  if (!p) return 0;
+  const BHState& h = *p;
+  return h.tables.bytes() + h.seg_of.bytes() + h.seg_minmax.bytes() + h.box.bytes() +
+         h.seg_root.bytes() + h.seg_end.bytes() + h.seg_depth.bytes() + h.mkeys.bytes() + h.mkeys_alt.bytes() + h.midx.bytes() +
+         h.midx_alt.bytes() + h.klo.bytes() + h.khi.bytes() + h.khi_alt.bytes() +
+         h.pidx.bytes() + h.pidx_alt.bytes() + h.sk.bytes() + h.sk_alt.bytes() + h.kseg.bytes() +
+         h.hist.bytes() + h.scan_ws.bytes() + h.lcp.bytes() + h.ncnt.bytes() + h.nstart.bytes() +
+         h.scalars.bytes() + h.node_com.bytes() + h.node_geom.bytes() + h.node_info.bytes() +
+         h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() + h.spm.bytes() +
+         h.inter_total.bytes();
+}
+
+size_t bh_bytes_estimate(int64_t n) { return (size_t)n * 480 + (64u << 10); }
+
+BHState* bh_state_new() { return new BHState(); }
+
+// Grows a buffer to hold n elements, with 1.5x headroom when it has to
+// reallocate (a reallocation synchronises the device).
+template <typename T>
+static T* grow(DevBuf<T>& b, size_t n) {
+  if (n <= b.cap && b.ptr) return b.ptr;
+  return b.ensure(std::max(n, b.cap + b.cap / 2));
+}
+
+size_t bh_segment_table_bytes(const int64_t* n_per, int nseg) {
+  int64_t ntask = 0;
+  for (int s = 0; s < nseg; ++s) ntask += ceil_div(n_per[s], 32);
+  return ((size_t)nseg * 2 + 1) * sizeof(int64_t) + (size_t)ntask * sizeof(WarpTask);
+}
+
+// Segment tables -- arena offsets, first concatenated index (prefix sums of
+// the sizes) and warp tasks -- go up in one copy; seg_of is derived on the
+// device.
+void bh_set_segments(BHState& h, const int64_t* off, const int64_t* n_per, int nseg,
+                     cudaStream_t st, char* staging) {
+  if (nseg < 1) fail(NBGB_ERR_INVALID_ARG, "Validation Error: no Barnes-Hut segment");
+  const size_t bytes = bh_segment_table_bytes(n_per, nseg);
+  if (!staging) {
+    NBGB_CUDA(cudaStreamSynchronize(st));  // the internal staging buffer is reused below
+    staging = h.h_tables.ensure(bytes);
+  }
+  int64_t* hoff = reinterpret_cast<int64_t*>(staging);
+  int64_t* hbase = hoff + nseg;
+  WarpTask* ht = reinterpret_cast<WarpTask*>(hbase + nseg + 1);
+  int64_t t = 0, n = 0;
+  for (int s = 0; s < nseg; ++s) {
+    if (n_per[s] < 1) fail(NBGB_ERR_INVALID_ARG, "Validation Error: empty Barnes-Hut segment");
+    hoff[s] = off[s];
+    hbase[s] = n;
+    for (int64_t f = n; f < n + n_per[s]; f += 32) ht[t++] = WarpTask{f, n + n_per[s], s, 0};
+    n += n_per[s];
+  }
+  hbase[nseg] = n;
+  char* d = grow(h.tables, bytes);
+  NBGB_CUDA(cudaMemcpyAsync(d, staging, bytes, cudaMemcpyHostToDevice, st));
+  h.nseg = nseg;
+  h.ntasks = t;
   h.n = n;
-  float* part = h.bbox_part.ensure((size_t)bbox_blocks(n) * 6);
-  BBox* box = h.box.ensure(1);
-  launch_bbox(pm, n, part, box, err, st);
-  uint32_t* hist = h.hist.ensure(radix_hist_elems(n));
-  uint32_t* sws = h.scan_ws.ensure(scan_workspace_elems((int64_t)radix_hist_elems(n)) +
-                                   scan_workspace_elems(n + 1));
-  // Path keys in index order, stable radix sort by the high key (levels
-  // 1..21, 8 passes), then bodies that share their high key are ordered by
-  // (low key, Morton key, index): the full path order with the reference's
-  // insertion order (stable Morton order) inside a shared depth-32 cell.
-  u64* lo = h.klo.ensure((size_t)n);
-  u64* hi = h.khi.ensure((size_t)n);
-  u64* hi2 = h.khi_alt.ensure((size_t)n);
-  uint32_t* pb = h.pidx.ensure((size_t)n);
-  uint32_t* pb2 = h.pidx_alt.ensure((size_t)n);
-  path_hi_index_kernel<<<grid1d(n), 256, 0, st>>>(pm, n, box, hi, pb);
+  if (n > h.reserve) h.reserve = std::max(n, h.reserve + h.reserve / 2);
+  h.seg_off_p = reinterpret_cast<int64_t*>(d);
+  h.seg_base_p = h.seg_off_p + nseg;
+  h.tasks_p = reinterpret_cast<WarpTask*>(h.seg_base_p + nseg + 1);
+  int32_t* so = grow(h.seg_of, (size_t)h.reserve);
+  seg_of_kernel<<<grid1d(n), 256, 0, st>>>(h.seg_base_p, nseg, n, so);
+  NBGB_LAUNCH_CHECK();
+}
+
+// Builds the trees of all segments (positions and masses read from `pm` at
+// each segment's offset).
+void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err) {
+  const int64_t n = h.n;
+  const int nseg = h.nseg;
+  const size_t R = (size_t)h.reserve;  // per-body buffers are sized for the reserve
+  SegView sv{h.seg_off_p, h.seg_base_p, h.seg_of.ptr, grow(h.box, (size_t)nseg)};
+  // 1. per-segment bounds and root cubes
+  uint32_t* mm = grow(h.seg_minmax, (size_t)nseg * 6);
+  NBGB_CUDA(cudaMemsetAsync(mm, 0xFF, (size_t)nseg * 3 * sizeof(uint32_t), st));
+  NBGB_CUDA(cudaMemsetAsync(mm + (size_t)nseg * 3, 0x00, (size_t)nseg * 3 * sizeof(uint32_t), st));
+  seg_bounds_kernel<<<(unsigned)ceil_div(n, 1024), 256, 0, st>>>(pm, sv, n, nseg, mm);
+  NBGB_LAUNCH_CHECK();
+  seg_box_kernel<<<(unsigned)ceil_div(nseg, 128), 128, 0, st>>>(mm, nseg, h.box.ptr, err);
+  NBGB_LAUNCH_CHECK();
+  // 2. keys and order
+  uint32_t* hist = grow(h.hist, radix_hist_elems((int64_t)R));
+  uint32_t* sws = grow(h.scan_ws, scan_workspace_elems((int64_t)radix_hist_elems((int64_t)R)) +
+                                      scan_workspace_elems((int64_t)R + 1));
+  u64* hi = grow(h.khi, R);
+  u64* hi2 = grow(h.khi_alt, R);
+  u64* lo = grow(h.klo, R);
+  uint32_t* pb = grow(h.pidx, R);
+  uint32_t* pb2 = grow(h.pidx_alt, R);
+  path_hi_index_kernel<<<grid1d(n), 256, 0, st>>>(pm, sv, n, hi, pb);
   NBGB_LAUNCH_CHECK();
   bool alt = false;
-  radix_sort_pairs<u64>(hi, hi2, pb, pb2, n, 0, 64, hist, sws, st, &alt);
-  h.body = alt ? pb2 : pb;
-  h.hi_sorted = alt ? hi2 : hi;
-  tie_order_kernel<<<grid1d(n), 256, 0, st>>>(pm, n, box, h.hi_sorted, const_cast<uint32_t*>(h.body));
+  radix_sort_pairs<u64>(hi, hi2, pb, pb2, n, 0, 64, hist, sws, st, &alt, err);
+  uint32_t* body = alt ? pb2 : pb;
+  uint32_t* body_other = alt ? pb : pb2;
+  if (nseg > 1) {
+    // stable sort by segment: (segment, path) order
+    uint32_t* sk = grow(h.sk, R);
+    uint32_t* sk2 = grow(h.sk_alt, R);
+    seg_key_kernel<<<grid1d(n), 256, 0, st>>>(body, h.seg_of.ptr, n, sk);
+    NBGB_LAUNCH_CHECK();
+    int bits = 1;
+    while (bits < 31 && (1 << bits) < nseg) ++bits;
+    bool alt2 = false;
+    radix_sort_pairs<uint32_t>(sk, sk2, body, body_other, n, 0, ((bits + 7) / 8) * 8, hist, sws,
+                               st, &alt2, err);
+    if (alt2) std::swap(body, body_other);
+  }
+  h.body = body;
+  int32_t* kseg = grow(h.kseg, R);
+  float4* spm = grow(h.spm, R);
+  path_final_kernel<<<grid1d(n), 256, 0, st>>>(pm, sv, body, n, kseg, hi, lo, spm);
+  NBGB_LAUNCH_CHECK();
+  tie_order_kernel<<<grid1d(n), 256, 0, st>>>(sv, n, kseg, hi, body, lo, spm);
   NBGB_LAUNCH_CHECK();
   h.keys_valid = false;  // Morton (key, index) pairs are produced on demand
-  float4* spm = h.spm.ensure((size_t)n);
-  path_final_kernel<<<grid1d(n), 256, 0, st>>>(pm, h.body, n, box, lo, spm);
-  NBGB_LAUNCH_CHECK();
-  // node counts, numbering, emission
-  uint8_t* lcp = h.lcp.ensure((size_t)n);
-  uint32_t* cnt = h.ncnt.ensure((size_t)n + 1);
-  uint32_t* nst = h.nstart.ensure((size_t)n + 1);
-  uint32_t* sc = h.scalars.ensure(2);
-  lcp_count_kernel<<<grid1d(n), 256, 0, st>>>(h.hi_sorted, lo, n, lcp, cnt);
+  // 3.-4. node counts, numbering, emission
+  uint8_t* lcp = grow(h.lcp, R);
+  uint32_t* cnt = grow(h.ncnt, R + 1);
+  uint32_t* nst = grow(h.nstart, R + 1);
+  uint32_t* sc = grow(h.scalars, 2);
+  lcp_count_kernel<<<grid1d(n), 256, 0, st>>>(kseg, hi, lo, n, lcp, cnt);
   NBGB_LAUNCH_CHECK();
   scan_exclusive_u32(cnt, nst, n + 1, sws, sc, st);
-  NBGB_CUDA(cudaMemsetAsync(sc + 1, 0, sizeof(uint32_t), st));
-  if (h.cap < 2 * n + 64) h.cap = 0;
-  if (h.cap == 0) h.cap = 3 * n + 64;
-  float4* geom = h.node_geom.ensure((size_t)h.cap);
-  float4* com = h.node_com.ensure((size_t)h.cap);
-  int4* info = h.node_info.ensure((size_t)h.cap);
-  int32_t* par = h.node_parent.ensure((size_t)h.cap);
-  int32_t* nch = h.node_nchild.ensure((size_t)h.cap);
-  int32_t* vis = h.node_visit.ensure((size_t)h.cap);
-  EmitArgs ea{lcp, h.hi_sorted, lo, nst, h.body, spm, box, n, h.cap, geom, info, vis, sc, err};
+  int32_t* sdepth = grow(h.seg_depth, (size_t)nseg);
+  NBGB_CUDA(cudaMemsetAsync(sdepth, 0, (size_t)nseg * sizeof(int32_t), st));
+  const int64_t min_cap = 2 * n + 64 * (int64_t)nseg;
+  if (h.cap < min_cap) h.cap = 3 * n + 64 * (int64_t)nseg;
+  float4* geom = grow(h.node_geom, (size_t)h.cap);
+  float4* com = grow(h.node_com, (size_t)h.cap);
+  int4* info = grow(h.node_info, (size_t)h.cap);
+  int32_t* par = grow(h.node_parent, (size_t)h.cap);
+  int32_t* nch = grow(h.node_nchild, (size_t)h.cap);
+  int32_t* vis = grow(h.node_visit, (size_t)h.cap);
+  EmitArgs ea{kseg, lcp, hi, lo, nst, spm, h.box.ptr, h.seg_base_p, n, h.cap, geom, info, par,
+              vis, grow(h.seg_root, (size_t)nseg), grow(h.seg_end, (size_t)nseg), sdepth, err};
   emit_nodes_kernel<<<grid1d(n), 256, 0, st>>>(ea);
   NBGB_LAUNCH_CHECK();
   link_kernel<<<grid1d(h.cap), 256, 0, st>>>(info, nst, n, h.cap, par, nch);
@@ -654,41 +894,9 @@ static void bh_build(nbgb_calculator* c, BHState& h, const float4* pm, int64_t n
   NBGB_LAUNCH_CHECK();
 }
 
-size_t bh_state_bytes(const BHState* p) {
-  if (!p) return 0;
-  const BHState& h = *p;
-  return h.bbox_part.bytes() + h.box.bytes() + h.mkeys.bytes() + h.mkeys_alt.bytes() +
-         h.midx.bytes() + h.midx_alt.bytes() + h.klo.bytes() + h.klo_alt.bytes() +
-         h.khi.bytes() + h.khi_alt.bytes() + h.pidx.bytes() + h.pidx_alt.bytes() +
-         h.hist.bytes() + h.scan_ws.bytes() + h.lcp.bytes() + h.ncnt.bytes() + h.nstart.bytes() +
-         h.scalars.bytes() + h.node_com.bytes() + h.node_geom.bytes() + h.node_info.bytes() +
-         h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() + h.spm.bytes();
-}
-
-// Node capacity that any realistic input fits (the canonical tree has ~1.5N
-// nodes; 4N + 64 leaves room for strongly clustered sets).  Used when the
-// calculator runs without per-call synchronization (no read-back to regrow).
-static int64_t bh_async_capacity(int64_t n) { return 4 * n + 64; }
-
-void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float* ay, float* az) {
-  if (!c->bh) c->bh.reset(new BHState());
-  BHState& h = *c->bh;
-  cudaStream_t st = c->stream;
-  const bool sync = (c->params.flags & NBGB_FLAG_SYNC) != 0;
-  if (!sync && h.cap < bh_async_capacity(n)) h.cap = bh_async_capacity(n);
-  for (int attempt = 0; attempt < 2; ++attempt) {
-    bh_build(c, h, pm, n);
-    if (!sync) break;  // capacity overflow surfaces through the device error word
-    // The node count is data dependent: read it back and regrow once if the
-    // capacity was too small (the kernels skipped their work in that case).
-    uint32_t* hs = h.h_scalars.ensure(2);
-    NBGB_CUDA(cudaMemcpyAsync(hs, h.scalars.ptr, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    NBGB_CUDA(cudaStreamSynchronize(st));
-    if ((int64_t)hs[0] <= h.cap) break;
-    // clear the capacity error raised by the emit kernel and grow
-    NBGB_CUDA(cudaMemsetAsync(c->err.ptr, 0, sizeof(uint32_t), st));
-    h.cap = (int64_t)hs[0] + (int64_t)hs[0] / 8 + 64;
-  }
+// Forces for every segment: acc written at each segment's arena offset.
+void bh_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, float* az, int32_t* counts,
+             unsigned long long* inter_total, cudaStream_t st) {
   WalkArgs w;
   w.com = h.node_com.ptr;
   w.geom = h.node_geom.ptr;
@@ -696,20 +904,26 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
   w.spm = h.spm.ptr;
   w.body = h.body;
   w.nstart = h.nstart.ptr;
-  w.n = n;
+  w.sv = SegView{h.seg_off_p, h.seg_base_p, h.seg_of.ptr, h.box.ptr};
+  w.tasks = h.tasks_p;
+  w.ntasks = h.ntasks;
+  w.seg_root = h.seg_root.ptr;
+  w.seg_end = h.seg_end.ptr;
+  w.n = h.n;
   w.cap = h.cap;
-  const float th = c->params.theta, eps = c->params.softening;
-  w.theta2 = th * th;
-  w.eps2 = eps * eps;
-  w.G = c->params.G;
-  w.leaf_cap = c->params.leaf_capacity;
+  w.theta2 = p.theta * p.theta;
+  w.eps2 = p.softening * p.softening;
+  w.G = p.G;
+  w.leaf_cap = p.leaf_capacity;
   w.ax = ax;
   w.ay = ay;
   w.az = az;
-  const bool count = (c->params.flags & NBGB_FLAG_COUNT_INTERACTIONS) != 0;
-  w.counts = count ? c->counts.ensure((size_t)n) : nullptr;
-  const bool bucket = c->params.leaf_capacity > 1;
-  const unsigned blocks = grid1d(n);
+  w.counts = counts;
+  w.inter_total = inter_total;
+  const bool count = counts != nullptr || inter_total != nullptr;
+  const bool bucket = p.leaf_capacity > 1;
+  const unsigned blocks = (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(h.ntasks * 32, 256), (int64_t)num_sms() * 32));
   if (count) {
     if (bucket) bh_walk_kernel<true, true><<<blocks, 256, 0, st>>>(w);
     else bh_walk_kernel<true, false><<<blocks, 256, 0, st>>>(w);
@@ -720,12 +934,47 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
   NBGB_LAUNCH_CHECK();
 }
 
+// Node capacity that any realistic input fits (the canonical tree has ~1.5N
+// nodes; 4N + 64 per segment leaves room for strongly clustered sets).  Used
+// when there is no per-call synchronization (no read-back to regrow).
+void bh_reserve_async(BHState& h) {
+  const int64_t c = 4 * h.reserve + 64 * (int64_t)std::max(h.nseg, 1);
+  if (h.cap < c) h.cap = std::max(c, h.cap + h.cap / 2);
+}
+
+// The calculator path: one segment at offset 0.
+void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float* ay, float* az) {
+  if (!c->bh) c->bh.reset(new BHState());
+  BHState& h = *c->bh;
+  cudaStream_t st = c->stream;
+  uint32_t* err = c->err.ensure(1);
+  if (h.nseg != 1 || h.n != n) {
+    const int64_t off = 0;
+    bh_set_segments(h, &off, &n, 1, st, nullptr);
+  }
+  const bool sync = (c->params.flags & NBGB_FLAG_SYNC) != 0;
+  if (!sync) bh_reserve_async(h);
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    bh_build(h, pm, st, err);
+    if (!sync) break;  // capacity overflow surfaces through the device error word
+    // The node count is data dependent: read it back and regrow once if the
+    // capacity was too small (the kernels skipped their work in that case).
+    uint32_t* hs = h.h_scalars.ensure(2);
+    NBGB_CUDA(cudaMemcpyAsync(hs, h.scalars.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    NBGB_CUDA(cudaStreamSynchronize(st));
+    if ((int64_t)hs[0] <= h.cap) break;
+    NBGB_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
+    h.cap = (int64_t)hs[0] + (int64_t)hs[0] / 8 + 64;
+  }
+  BHWalkParams wp{c->params.G, c->params.softening, c->params.theta, c->params.leaf_capacity};
+  const bool count = (c->params.flags & NBGB_FLAG_COUNT_INTERACTIONS) != 0;
+  bh_walk(h, wp, ax, ay, az, count ? c->counts.ensure((size_t)n) : nullptr, nullptr, st);
+}
+
 // ------------------------------------------------------------- export --
 __global__ void export_nodes_kernel(const float4* __restrict__ com, const float4* __restrict__ geom,
-                                    const int4* __restrict__ info, const int32_t* __restrict__ parent,
-                                    const uint32_t* __restrict__ body, const u64* __restrict__ hi,
-                                    const u64* __restrict__ lo, int64_t total,
-                                    nbgb_octree_node* __restrict__ out) {
+                                    const int4* __restrict__ info, const uint32_t* __restrict__ body,
+                                    int64_t total, nbgb_octree_node* __restrict__ out) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total;
        p += (int64_t)gridDim.x * blockDim.x) {
     const int4 in = info[p];
@@ -751,8 +1000,9 @@ __global__ void export_children_kernel(const int4* __restrict__ info,
                                        const int32_t* __restrict__ parent,
                                        const u64* __restrict__ hi, const u64* __restrict__ lo,
                                        int64_t total, nbgb_octree_node* __restrict__ out) {
-  for (int64_t p = 1 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total;
        p += (int64_t)gridDim.x * blockDim.x) {
+    if (parent[p] < 0) continue;  // a root
     const int4 in = info[p];
     const int d = in.w >> 8;
     const int64_t f = in.y;
@@ -771,12 +1021,14 @@ extern "C" {
 nbgb_status nbgb_bh_tree_stats(nbgb_calculator* c, int32_t* node_count, int32_t* max_depth) {
   if (!c || !c->bh || c->method != NBGB_BARNES_HUT) return NBGB_ERR_INVALID_ARG;
   BHState& h = *c->bh;
-  uint32_t s[2] = {0, 0};
+  uint32_t total = 0;
+  int32_t depth = 0;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return NBGB_ERR_CUDA;
-  if (cudaMemcpy(s, h.scalars.ptr, sizeof s, cudaMemcpyDeviceToHost) != cudaSuccess)
+  if (cudaMemcpy(&total, h.scalars.ptr, sizeof total, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(&depth, h.seg_depth.ptr, sizeof depth, cudaMemcpyDeviceToHost) != cudaSuccess)
     return NBGB_ERR_CUDA;
-  if (node_count) *node_count = (int32_t)s[0];
-  if (max_depth) *max_depth = (int32_t)s[1];
+  if (node_count) *node_count = (int32_t)total;
+  if (max_depth) *max_depth = depth;
   return NBGB_OK;
 }
 
@@ -784,7 +1036,7 @@ nbgb_status nbgb_bh_copy_sorted_keys(nbgb_calculator* c, uint32_t* keys, int32_t
                                      size_t n) {
   if (!c || !c->bh || c->method != NBGB_BARNES_HUT) return NBGB_ERR_INVALID_ARG;
   BHState& h = *c->bh;
-  if (n != (size_t)h.n) return NBGB_ERR_INVALID_ARG;
+  if (n != (size_t)h.n || h.nseg != 1) return NBGB_ERR_INVALID_ARG;
   if (!h.keys_valid) {
     // The reference's Morton keys and their stable sort
     // (force_barnes_hut.cu:308-328), from the bodies of the last build.
@@ -817,20 +1069,20 @@ nbgb_status nbgb_bh_copy_sorted_keys(nbgb_calculator* c, uint32_t* keys, int32_t
 nbgb_status nbgb_bh_copy_nodes(nbgb_calculator* c, nbgb_octree_node* nodes, size_t capacity) {
   if (!c || !c->bh || c->method != NBGB_BARNES_HUT || !nodes) return NBGB_ERR_INVALID_ARG;
   BHState& h = *c->bh;
-  uint32_t s[2] = {0, 0};
+  uint32_t total32 = 0;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return NBGB_ERR_CUDA;
-  if (cudaMemcpy(s, h.scalars.ptr, sizeof s, cudaMemcpyDeviceToHost) != cudaSuccess)
+  if (cudaMemcpy(&total32, h.scalars.ptr, sizeof total32, cudaMemcpyDeviceToHost) != cudaSuccess)
     return NBGB_ERR_CUDA;
-  const int64_t total = s[0];
+  const int64_t total = total32;
   if ((size_t)total > capacity || total > h.cap) return NBGB_ERR_INVALID_ARG;
   nbgb_octree_node* d = nullptr;
-  if (cudaMalloc(&d, (size_t)total * sizeof(nbgb_octree_node)) != cudaSuccess) return NBGB_ERR_OOM;
+  if (cudaMalloc(&d, (size_t)std::max<int64_t>(total, 1) * sizeof(nbgb_octree_node)) != cudaSuccess)
+    return NBGB_ERR_OOM;
   unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, 256), 4096));
   export_nodes_kernel<<<blocks, 256, 0, c->stream>>>(h.node_com.ptr, h.node_geom.ptr,
-                                                     h.node_info.ptr, h.node_parent.ptr, h.body,
-                                                     h.hi_sorted, h.klo.ptr, total, d);
+                                                     h.node_info.ptr, h.body, total, d);
   export_children_kernel<<<blocks, 256, 0, c->stream>>>(h.node_info.ptr, h.node_parent.ptr,
-                                                        h.hi_sorted, h.klo.ptr, total, d);
+                                                        h.khi.ptr, h.klo.ptr, total, d);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e == cudaSuccess)

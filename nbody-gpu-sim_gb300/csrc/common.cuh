@@ -41,7 +41,14 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
 }
 
 #define NBGB_CUDA(call) ::nbgb::cuda_check((call), #call, __FILE__, __LINE__)
-#define NBGB_LAUNCH_CHECK() ::nbgb::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__)
+// Kernel launches issued by this thread (every launch site is followed by
+// NBGB_LAUNCH_CHECK); engines report per-call deltas of it.
+inline thread_local int64_t t_launches = 0;
+#define NBGB_LAUNCH_CHECK()                                                              \
+  do {                                                                                   \
+    ++::nbgb::t_launches;                                                                \
+    ::nbgb::cuda_check(cudaGetLastError(), "kernel launch", __FILE__, __LINE__);         \
+  } while (0)
 
 // ---------------------------------------------------------------------------
 // Device error word.  Kernels never trap: a bounded wait that runs out, or a

@@ -352,6 +352,98 @@ void launch_potential(const float4* src, int64_t n, float eps2, double* partials
   NBGB_LAUNCH_CHECK();
 }
 
+// ----------------------------------------------- FP64-state kernels --
+// Forces and potential from FP64 positions in FP64 arithmetic: the
+// full-FP64 system variant and the energy of every FP64-state system.
+// 256-body tiles of (x, y, z, m) in shared memory, one target per thread,
+// self excluded by index, rsqrt from the CUDA math library.
+__global__ void __launch_bounds__(256) direct_f64_state_kernel(
+    const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
+    const float4* __restrict__ pm, int64_t n, double G, double eps2, double* __restrict__ ax,
+    double* __restrict__ ay, double* __restrict__ az) {
+  __shared__ double4 s_j[256];
+  for (int64_t base = (int64_t)blockIdx.x * 256; base < n; base += (int64_t)gridDim.x * 256) {
+    const int64_t i = base + threadIdx.x;
+    const bool valid = i < n;
+    const double xi = valid ? x[i] : 0.0, yi = valid ? y[i] : 0.0, zi = valid ? z[i] : 0.0;
+    double sx = 0.0, sy = 0.0, sz = 0.0;
+    for (int64_t c = 0; c < n; c += 256) {
+      __syncthreads();
+      const int64_t j = c + threadIdx.x;
+      s_j[threadIdx.x] = (j < n) ? make_double4(x[j], y[j], z[j], (double)pm[j].w)
+                                 : make_double4(0.0, 0.0, 0.0, 0.0);
+      __syncthreads();
+      const int lim = (int)imin64(256, n - c);
+      for (int k = 0; k < lim; ++k) {
+        if (c + k == i) continue;
+        const double4 q = s_j[k];
+        const double dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
+        const double d2 = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
+        const double r = rsqrt(d2);
+        const double f = q.w * r * r * r;
+        sx = fma(f, dx, sx);
+        sy = fma(f, dy, sy);
+        sz = fma(f, dz, sz);
+      }
+    }
+    if (valid) {
+      ax[i] = G * sx;
+      ay[i] = G * sy;
+      az[i] = G * sz;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) pe_f64_kernel(const double* __restrict__ x,
+                                                     const double* __restrict__ y,
+                                                     const double* __restrict__ z,
+                                                     const float4* __restrict__ pm, int64_t n,
+                                                     double eps2, double* partials) {
+  __shared__ double4 s_j[256];
+  double acc[1] = {0.0};
+  for (int64_t base = (int64_t)blockIdx.x * 256; base < n; base += (int64_t)gridDim.x * 256) {
+    const int64_t i = base + threadIdx.x;
+    const bool valid = i < n;
+    const double xi = valid ? x[i] : 0.0, yi = valid ? y[i] : 0.0, zi = valid ? z[i] : 0.0;
+    double s = 0.0;
+    for (int64_t c = 0; c < n; c += 256) {
+      __syncthreads();
+      const int64_t j = c + threadIdx.x;
+      s_j[threadIdx.x] = (j < n) ? make_double4(x[j], y[j], z[j], (double)pm[j].w)
+                                 : make_double4(0.0, 0.0, 0.0, 0.0);
+      __syncthreads();
+      const int lim = (int)imin64(256, n - c);
+      for (int k = 0; k < lim; ++k) {
+        if (c + k == i) continue;
+        const double4 q = s_j[k];
+        const double dx = q.x - xi, dy = q.y - yi, dz = q.z - zi;
+        s -= q.w * rsqrt(fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2))));
+      }
+    }
+    if (valid) acc[0] += 0.5 * (double)pm[i].w * s;
+  }
+  block_reduce_store<1>(acc, partials);
+}
+
+void launch_direct_f64_state(const double* x, const double* y, const double* z, const float4* pm,
+                             int64_t n, double G, double eps2, double* ax, double* ay, double* az,
+                             cudaStream_t st) {
+  if (n <= 0) return;
+  const unsigned blocks =
+      (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)num_sms() * 8));
+  direct_f64_state_kernel<<<blocks, 256, 0, st>>>(x, y, z, pm, n, G, eps2, ax, ay, az);
+  NBGB_LAUNCH_CHECK();
+}
+
+void launch_potential_f64(const double* x, const double* y, const double* z, const float4* pm,
+                          int64_t n, double eps2, double* partials, int nblocks, double* out,
+                          cudaStream_t st) {
+  pe_f64_kernel<<<nblocks, 256, 0, st>>>(x, y, z, pm, n, eps2, partials);
+  NBGB_LAUNCH_CHECK();
+  finish_reduce_kernel<1><<<1, 256, 0, st>>>(partials, nblocks, out);
+  NBGB_LAUNCH_CHECK();
+}
+
 }  // namespace nbgb
 
 // ---------------------------------------------------------------------------

@@ -10,14 +10,19 @@
 //             bounds test); admission is first-fit within the HBM budget.
 //   tick      1. one kick-drift kernel over every resident body (per-system
 //                kick: half on the first step, full afterwards);
-//             2. Barnes-Hut systems: each system's tree build + walk is a
-//                CUDA graph captured at admission, launched on a stream pool
-//                (overlaps with everything else on the device);
+//             2. Barnes-Hut systems: ONE build + walk over all of them (each
+//                system a segment of one key sort; trees and interaction
+//                sets per system identical to the single-system path), on
+//                a side stream that overlaps the direct kernel; captured as
+//                a CUDA graph while the Barnes-Hut resident set is stable;
 //             3. direct systems: one persistent kernel whose CTAs pull work
 //                items (system, 32..1024-target tile) from a queue spanning
 //                all direct systems, largest first;
 //             4. retirement: final half kick and an async copy of the state
 //                of systems that finished, then their memory is reused.
+//   admission a newly admitted system joins the next tick with a zero kick
+//             and drift: that tick only computes its a(0) inside the batched
+//             passes, so admission launches nothing per system.
 //   autotune  the direct kernel's configuration (threads per CTA = warps per
 //             tile, targets per thread, scalar or packed FP32x2) is picked
 //             by timing every candidate on the current mix; re-tuned when
@@ -28,14 +33,13 @@
 #include <memory>
 #include <vector>
 
+#include "bh.cuh"
 #include "common.cuh"
 #include "direct_core.cuh"
 #include "kernels.cuh"
 #include "runtime.cuh"
 
 namespace nbgb {
-
-size_t bh_state_bytes(const BHState* p);  // bh.cu
 
 constexpr int64_t kChunk = 256;  // arena granularity (== kDirTile)
 constexpr int kTimingRing = 8;   // direct-kernel event pairs in flight
@@ -233,17 +237,10 @@ struct ResidentSystem {
   float dt;
   int slot;
   nbgb_method method;
-  bool pending_half = false;
-  double bh_inter_per_step = 0.0;
+  bool fresh = true;          // admitted, a(0) not computed yet
+  bool pending_half = false;  // the previous step's closing half kick is still due
   size_t bytes = 0;
-  // Barnes-Hut
-  nbgb_calculator* calc = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t done_evt = nullptr;
   int64_t tick_admitted = 0;
-  int64_t graph_kernels = 0;  // kernel nodes in the captured step graph
 };
 
 // Host-to-device table uploads: the host runs ahead of the device, so a
@@ -265,6 +262,10 @@ struct UploadRing {
   }
   void upload(void* dst, size_t bytes, cudaStream_t st) {
     if (bytes) NBGB_CUDA(cudaMemcpyAsync(dst, buf[cur].ptr, bytes, cudaMemcpyHostToDevice, st));
+    mark(st);
+  }
+  // The current buffer's reader(s) were enqueued on `st` by the caller.
+  void mark(cudaStream_t st) {
     NBGB_CUDA(cudaEventRecord(ev[cur], st));
     used[cur] = true;
   }
@@ -289,8 +290,18 @@ struct nbgb_ensemble {
   nbgb_ensemble_config cfg{};
   int device = 0;
   cudaStream_t main = nullptr;
-  std::vector<cudaStream_t> pool;
-  int pool_next = 0;
+  // batched Barnes-Hut pass
+  cudaStream_t bh_stream = nullptr;
+  std::unique_ptr<BHState, BHDeleter> bh;
+  DevBuf<unsigned long long> d_bh_inter;  // interactions summed by the walks
+  UploadRing up_bh;
+  bool bh_dirty = true;   // Barnes-Hut resident set changed
+  int64_t bh_n = 0;       // bodies in the Barnes-Hut segments
+  int bh_stable = 0;      // ticks since the set last changed
+  cudaGraph_t bh_graph = nullptr;
+  cudaGraphExec_t bh_exec = nullptr;
+  int64_t bh_graph_kernels = 0;
+  cudaEvent_t ev_bh = nullptr;
   // arena
   int64_t cap = 0;  // bodies
   DevBuf<double> x, y, z, vx, vy, vz;
@@ -377,10 +388,9 @@ static void arena_free(nbgb_ensemble* e, int64_t off, int64_t n_pad) {
 
 static size_t arena_bytes_per_body() { return 6 * sizeof(double) + 3 * sizeof(float) + sizeof(float4); }
 
-// Rough footprint of a Barnes-Hut system's tree workspace (bh.cu buffers at
-// the asynchronous node capacity 4N + 64): used for admission before the
-// exact figure is known.
-static size_t bh_estimate_bytes(int64_t n) { return (size_t)n * 420 + (1u << 20); }
+// Share of the batched tree workspace reserved per Barnes-Hut system
+// (buffers at the asynchronous node capacity, with growth headroom).
+static size_t bh_estimate_bytes(int64_t n) { return bh_bytes_estimate(n); }
 
 static nbgb_method method_for(const nbgb_ensemble* e, int64_t n) {
   return n <= e->cfg.direct_max_n ? NBGB_DIRECT_N2 : NBGB_BARNES_HUT;
@@ -421,86 +431,76 @@ static void rebuild_tables(nbgb_ensemble* e) {
   e->tables_dirty = false;
 }
 
-static void compute_initial_direct(nbgb_ensemble* e, ResidentSystem& s) {
-  DirectPlan p = plan_direct(s.n, s.n, DirectVariant::kScalar4);
-  float4* part = p.splits > 1 ? e->part.ensure((size_t)p.splits * p.n_tgt_pad) : nullptr;
-  launch_direct(p, e->pm.ptr + s.off, e->pm.ptr + s.off, s.n, e->cfg.G,
-                e->cfg.softening * e->cfg.softening, true, part, e->ax.ptr + s.off,
-                e->ay.ptr + s.off, e->az.ptr + s.off, e->d_err.ptr, e->main);
+// Segment tables of the batched Barnes-Hut pass (all resident Barnes-Hut
+// systems, in resident order), uploaded through the staging ring.
+static void bh_tables(nbgb_ensemble* e) {
+  std::vector<int64_t> off, cnt;
+  for (auto& s : e->resident)
+    if (s->method == NBGB_BARNES_HUT) {
+      off.push_back(s->off);
+      cnt.push_back(s->n);
+    }
+  e->bh_n = 0;
+  for (int64_t c : cnt) e->bh_n += c;
+  e->bh_dirty = false;
+  e->bh_stable = 0;
+  if (e->bh_exec) {
+    cudaGraphExecDestroy(e->bh_exec);
+    e->bh_exec = nullptr;
+  }
+  if (e->bh_graph) {
+    cudaGraphDestroy(e->bh_graph);
+    e->bh_graph = nullptr;
+  }
+  if (off.empty()) return;
+  if (!e->bh) e->bh.reset(bh_state_new());
+  const int nseg = (int)off.size();
+  char* stg = static_cast<char*>(e->up_bh.acquire(bh_segment_table_bytes(cnt.data(), nseg)));
+  bh_set_segments(*e->bh, off.data(), cnt.data(), nseg, e->bh_stream, stg);
+  e->up_bh.mark(e->bh_stream);
+  bh_reserve_async(*e->bh);
 }
 
-static void setup_bh(nbgb_ensemble* e, ResidentSystem& s) {
-  nbgb_params p;
-  nbgb_params_default(&p);
-  p.G = e->cfg.G;
-  p.softening = e->cfg.softening;
-  p.theta = e->cfg.theta;
-  p.leaf_capacity = e->cfg.leaf_capacity;
-  p.flags = NBGB_FLAG_COMPENSATED | NBGB_FLAG_COUNT_INTERACTIONS;
-  nbgb_calculator* c = nullptr;
-  nbgb_status st = nbgb_calculator_create(NBGB_BARNES_HUT, &p, &c);
-  if (st != NBGB_OK) fail(st, nbgb_last_error());
-  s.calc = c;
-  s.stream = e->pool[e->pool_next++ % e->pool.size()];
-  if (c->own_stream) {
-    NBGB_CUDA(cudaStreamSynchronize(c->stream));  // its error-word reset
-    NBGB_CUDA(cudaStreamDestroy(c->stream));
-  }
-  c->own_stream = false;
-  c->stream = s.stream;
-  // the state must be on the device before the tree kernels read it
-  cudaEvent_t ev;
-  NBGB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-  NBGB_CUDA(cudaEventRecord(ev, e->main));
-  NBGB_CUDA(cudaStreamWaitEvent(s.stream, ev, 0));
-  NBGB_CUDA(cudaEventDestroy(ev));
-  // warm-up: allocates every buffer and computes a(0); counts interactions once
-  bh_forces(c, e->pm.ptr + s.off, s.n, e->ax.ptr + s.off, e->ay.ptr + s.off, e->az.ptr + s.off);
-  std::vector<int32_t> cnt((size_t)s.n);
-  NBGB_CUDA(cudaMemcpyAsync(cnt.data(), c->counts.ptr, (size_t)s.n * 4, cudaMemcpyDeviceToHost, s.stream));
-  NBGB_CUDA(cudaStreamSynchronize(s.stream));
-  double tot = 0.0;
-  for (int32_t v : cnt) tot += v;
-  s.bh_inter_per_step = tot;
-  c->params.flags = NBGB_FLAG_COMPENSATED;  // no counting in the steady state
-  s.bytes = bh_state_bytes(c->bh.get()) + c->counts.bytes();
-  if (e->cfg.use_graphs) {
-    NBGB_CUDA(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
-    try {
-      bh_forces(c, e->pm.ptr + s.off, s.n, e->ax.ptr + s.off, e->ay.ptr + s.off, e->az.ptr + s.off);
-    } catch (...) {
-      cudaGraph_t g;
-      cudaStreamEndCapture(s.stream, &g);
-      if (g) cudaGraphDestroy(g);
-      throw;
-    }
-    NBGB_CUDA(cudaStreamEndCapture(s.stream, &s.graph));
-    NBGB_CUDA(cudaGraphInstantiate(&s.exec, s.graph, 0));
-    size_t nn = 0;
-    NBGB_CUDA(cudaGraphGetNodes(s.graph, nullptr, &nn));
-    std::vector<cudaGraphNode_t> nodes(nn);
-    NBGB_CUDA(cudaGraphGetNodes(s.graph, nodes.data(), &nn));
-    for (cudaGraphNode_t nd : nodes) {
-      cudaGraphNodeType t;
-      NBGB_CUDA(cudaGraphNodeGetType(nd, &t));
-      if (t == cudaGraphNodeTypeKernel) ++s.graph_kernels;
-    }
-  }
+// Build + walk of every resident Barnes-Hut system, enqueued on bh_stream.
+static void bh_pass(nbgb_ensemble* e) {
+  const BHWalkParams wp{e->cfg.G, e->cfg.softening, e->cfg.theta, e->cfg.leaf_capacity};
+  bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr);
+  bh_walk(*e->bh, wp, e->ax.ptr, e->ay.ptr, e->az.ptr, nullptr, e->d_bh_inter.ptr, e->bh_stream);
 }
 
-static void release_system(ResidentSystem& s) {
-  if (s.exec) cudaGraphExecDestroy(s.exec);
-  if (s.graph) cudaGraphDestroy(s.graph);
-  s.exec = nullptr;
-  s.graph = nullptr;
-  if (s.calc) nbgb_calculator_destroy(s.calc);  // its stream belongs to the pool
-  s.calc = nullptr;
+// Launches the pass: eagerly right after the set changed, then (with graphs
+// enabled) as a graph captured on the first stable tick, when every buffer
+// of the pass has been allocated.  Returns the kernels the graph launched.
+static int64_t run_bh_pass(nbgb_ensemble* e) {
+  if (e->bh_exec) {
+    NBGB_CUDA(cudaGraphLaunch(e->bh_exec, e->bh_stream));
+    return e->bh_graph_kernels;
+  }
+  if (!e->cfg.use_graphs || e->bh_stable < 1) {
+    bh_pass(e);
+    return 0;
+  }
+  const int64_t l0 = t_launches;
+  NBGB_CUDA(cudaStreamBeginCapture(e->bh_stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    bh_pass(e);
+  } catch (...) {
+    cudaGraph_t g = nullptr;
+    cudaStreamEndCapture(e->bh_stream, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  NBGB_CUDA(cudaStreamEndCapture(e->bh_stream, &e->bh_graph));
+  NBGB_CUDA(cudaGraphInstantiate(&e->bh_exec, e->bh_graph, 0));
+  e->bh_graph_kernels = t_launches - l0;
+  t_launches = l0;  // captured, not launched: the graph launch below counts them
+  NBGB_CUDA(cudaGraphLaunch(e->bh_exec, e->bh_stream));
+  return e->bh_graph_kernels;
 }
 
 // Admits, in FIFO order, every queued request that fits the resident cap,
 // the HBM budget and the arena.  All admitted states go up in one staging
-// copy; a(0) is computed per system (direct: one plain launch; Barnes-Hut:
-// warm-up call that also sizes the tree and captures the step graph).
+// copy; a(0) is computed by the next tick's batched passes.
 static void admit_batch(nbgb_ensemble* e) {
   struct Pending {
     std::unique_ptr<ResidentSystem> s;
@@ -561,16 +561,10 @@ static void admit_batch(nbgb_ensemble* e) {
   }
   for (auto& p : batch) {
     ResidentSystem& s = *p.s;
-    if (s.method == NBGB_DIRECT_N2) {
-      compute_initial_direct(e, s);
+    if (s.method == NBGB_DIRECT_N2)
       e->direct_load += (double)s.n * (double)s.n;
-    } else {
-      const size_t est = s.bytes;
-      s.bytes = 0;
-      setup_bh(e, s);
-      s.bytes += (size_t)s.n_pad * arena_bytes_per_body();
-      e->bytes_reserved = e->bytes_reserved - est + s.bytes;
-    }
+    else
+      e->bh_dirty = true;
     e->resident.push_back(std::move(p.s));
     e->st.admitted++;
   }
@@ -581,7 +575,6 @@ static void retire(nbgb_ensemble* e, std::unique_ptr<ResidentSystem> s) {
   // final half kick, then copy the state out
   launch_kick(s->n, e->vx.ptr + s->off, e->vy.ptr + s->off, e->vz.ptr + s->off, e->ax.ptr + s->off,
               e->ay.ptr + s->off, e->az.ptr + s->off, 0.5 * (double)s->dt, e->main);
-  e->st.kernel_launches += 1;
   Retiring r;
   r.res.request_id = s->id;
   r.res.count = s->n;
@@ -600,20 +593,20 @@ static void retire(nbgb_ensemble* e, std::unique_ptr<ResidentSystem> s) {
   NBGB_CUDA(cudaMemcpyAsync(hf + 2 * n, e->az.ptr + s->off, n * 4, cudaMemcpyDeviceToHost, e->main));
   NBGB_CUDA(cudaMemcpy2DAsync(hf + 3 * n, sizeof(float), reinterpret_cast<const char*>(e->pm.ptr + s->off) + 12,
                               sizeof(float4), sizeof(float), n, cudaMemcpyDeviceToHost, e->main));
-  // device error words (ensemble; the system's own tree calculator)
+  // device error word (bounded waits, tree capacity, non-finite bounds)
   uint32_t* herr = reinterpret_cast<uint32_t*>(hf + 4 * n);
   NBGB_CUDA(cudaMemcpyAsync(herr, e->d_err.ptr, 4, cudaMemcpyDeviceToHost, e->main));
-  if (s->calc)
-    NBGB_CUDA(cudaMemcpyAsync(herr + 1, s->calc->err.ptr, 4, cudaMemcpyDeviceToHost, e->main));
-  else
-    herr[1] = 0;
+  herr[1] = 0;
   NBGB_CUDA(cudaEventCreateWithFlags(&r.evt, cudaEventDisableTiming));
   NBGB_CUDA(cudaEventRecord(r.evt, e->main));
   // device work that reuses this memory is ordered after the copies on main
   arena_free(e, s->off, s->n_pad);
   e->bytes_reserved -= s->bytes;
   e->free_slots.push_back(s->slot);
-  if (s->method == NBGB_DIRECT_N2) e->direct_load -= (double)s->n * (double)s->n;
+  if (s->method == NBGB_DIRECT_N2)
+    e->direct_load -= (double)s->n * (double)s->n;
+  else
+    e->bh_dirty = true;
   e->st.retired++;
   r.sys = std::move(s);
   e->retiring.push_back(std::move(r));
@@ -684,15 +677,25 @@ static void maybe_start_tuning(nbgb_ensemble* e) {
 }
 
 static void run_tick(nbgb_ensemble* e) {
+  const int64_t l0 = t_launches;
+  int64_t graph_kernels = 0;
   admit_batch(e);
   maybe_start_tuning(e);
   tune_select(e);
-  if (e->resident.empty()) return;
+  if (e->resident.empty()) {
+    e->st.kernel_launches += t_launches - l0;
+    return;
+  }
   if (e->tables_dirty || e->items_config != e->config) rebuild_tables(e);
-  // per-slot kick factors
+  if (e->bh_dirty) bh_tables(e);
+  // per-slot kick factors: a fresh system neither kicks nor drifts (its
+  // a(0) is computed below); afterwards the closing half kick of the last
+  // step and the opening half kick of this one are merged
   SlotParams* sp = static_cast<SlotParams*>(e->up_slot.acquire((size_t)std::max(e->n_slots, 1) * sizeof(SlotParams)));
   for (auto& s : e->resident)
-    sp[s->slot] = SlotParams{s->pending_half ? (double)s->dt : 0.5 * (double)s->dt, (double)s->dt};
+    sp[s->slot] = s->fresh ? SlotParams{0.0, 0.0}
+                           : SlotParams{s->pending_half ? (double)s->dt : 0.5 * (double)s->dt,
+                                        (double)s->dt};
   SlotParams* dsp = e->d_slot.ensure((size_t)std::max(e->n_slots, 1));
   e->up_slot.upload(dsp, (size_t)e->n_slots * sizeof(SlotParams), e->main);
   // 1. kick-drift for everything resident
@@ -704,18 +707,13 @@ static void run_tick(nbgb_ensemble* e) {
     NBGB_LAUNCH_CHECK();
   }
   NBGB_CUDA(cudaEventRecord(e->ev_kd, e->main));
-  // 2. Barnes-Hut systems on the stream pool
-  std::vector<cudaStream_t> used;
-  for (auto& s : e->resident) {
-    if (s->method != NBGB_BARNES_HUT) continue;
-    NBGB_CUDA(cudaStreamWaitEvent(s->stream, e->ev_kd, 0));
-    if (s->exec) {
-      NBGB_CUDA(cudaGraphLaunch(s->exec, s->stream));
-    } else {
-      bh_forces(s->calc, e->pm.ptr + s->off, s->n, e->ax.ptr + s->off, e->ay.ptr + s->off,
-                e->az.ptr + s->off);
-    }
-    if (std::find(used.begin(), used.end(), s->stream) == used.end()) used.push_back(s->stream);
+  // 2. all Barnes-Hut systems: one batched pass on the side stream
+  const bool bh_work = e->bh_n > 0;
+  if (bh_work) {
+    NBGB_CUDA(cudaStreamWaitEvent(e->bh_stream, e->ev_kd, 0));
+    graph_kernels = run_bh_pass(e);
+    NBGB_CUDA(cudaEventRecord(e->ev_bh, e->bh_stream));
+    e->bh_stable++;
   }
   // 3. direct systems: persistent work-queue kernel (always timed)
   if (e->n_items) {
@@ -737,28 +735,20 @@ static void run_tick(nbgb_ensemble* e) {
     e->tev_used[k] = true;
     e->tev_next++;
     if (e->tuning) e->tune_tick++;
+    e->st.direct_interactions += inter;
   }
-  // join the pool streams back into main
-  for (cudaStream_t s : used) {
-    cudaEvent_t ev;
-    NBGB_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    NBGB_CUDA(cudaEventRecord(ev, s));
-    NBGB_CUDA(cudaStreamWaitEvent(e->main, ev, 0));
-    NBGB_CUDA(cudaEventDestroy(ev));
-  }
+  if (bh_work) NBGB_CUDA(cudaStreamWaitEvent(e->main, e->ev_bh, 0));
   // 4. bookkeeping and retirement
   e->st.ticks++;
-  e->st.kernel_launches += (e->n_kd ? 1 : 0) + (e->n_items ? 1 : 0);
   std::vector<std::unique_ptr<ResidentSystem>> keep;
   for (auto& s : e->resident) {
-    if (s->method == NBGB_BARNES_HUT) e->st.kernel_launches += s->graph_kernels;
+    if (s->fresh) {
+      s->fresh = false;
+      continue;
+    }
     s->done++;
     s->pending_half = true;
     e->st.particle_steps += s->n;
-    if (s->method == NBGB_DIRECT_N2)
-      e->st.direct_interactions += (double)s->n * (double)(s->n - 1);
-    else
-      e->st.bh_interactions += s->bh_inter_per_step;
   }
   for (auto& s : e->resident) {
     if (s->done >= s->steps)
@@ -767,6 +757,7 @@ static void run_tick(nbgb_ensemble* e) {
       keep.push_back(std::move(s));
   }
   e->resident.swap(keep);
+  e->st.kernel_launches += t_launches - l0 + graph_kernels;
 }
 
 }  // namespace nbgb
@@ -821,11 +812,7 @@ nbgb_status nbgb_ensemble_create(const nbgb_ensemble_config* cfg, nbgb_ensemble*
     e->cfg = c;
     NBGB_CUDA(cudaGetDevice(&e->device));
     NBGB_CUDA(cudaStreamCreateWithFlags(&e->main, cudaStreamNonBlocking));
-    for (int k = 0; k < 16; ++k) {
-      cudaStream_t s;
-      NBGB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-      e->pool.push_back(s);
-    }
+    NBGB_CUDA(cudaStreamCreateWithFlags(&e->bh_stream, cudaStreamNonBlocking));
     // arena: a quarter of the budget holds body state; the rest is for trees
     e->cap = std::max<int64_t>(kChunk, (int64_t)(c.hbm_budget_bytes / 4 / arena_bytes_per_body()) / kChunk * kChunk);
     e->x.ensure((size_t)e->cap);
@@ -847,6 +834,9 @@ nbgb_status nbgb_ensemble_create(const nbgb_ensemble_config* cfg, nbgb_ensemble*
       NBGB_CUDA(cudaEventCreate(&e->tev1[k]));
     }
     NBGB_CUDA(cudaEventCreateWithFlags(&e->ev_kd, cudaEventDisableTiming));
+    NBGB_CUDA(cudaEventCreateWithFlags(&e->ev_bh, cudaEventDisableTiming));
+    e->d_bh_inter.ensure(1);
+    NBGB_CUDA(cudaMemset(e->d_bh_inter.ptr, 0, sizeof(unsigned long long)));
     e->config = c.direct_config >= 0 ? c.direct_config : 0;
     *out = e.release();
   });
@@ -856,13 +846,15 @@ nbgb_status nbgb_ensemble_destroy(nbgb_ensemble* e) {
   return ens_guard([&] {
     if (!e) return;
     cudaDeviceSynchronize();
-    for (auto& s : e->resident) release_system(*s);
     for (auto& r : e->retiring) {
-      if (r.sys) release_system(*r.sys);
       if (r.h_state) cudaFreeHost(r.h_state);
       if (r.evt) cudaEventDestroy(r.evt);
     }
-    for (cudaStream_t s : e->pool) cudaStreamDestroy(s);
+    if (e->bh_exec) cudaGraphExecDestroy(e->bh_exec);
+    if (e->bh_graph) cudaGraphDestroy(e->bh_graph);
+    e->bh.reset();
+    cudaStreamDestroy(e->bh_stream);
+    cudaEventDestroy(e->ev_bh);
     for (int k = 0; k < kTimingRing; ++k) {
       cudaEventDestroy(e->tev0[k]);
       cudaEventDestroy(e->tev1[k]);
@@ -926,7 +918,7 @@ nbgb_status nbgb_ensemble_poll(nbgb_ensemble* e, nbgb_ensemble_result* result,
   const uint32_t* herr =
       reinterpret_cast<const uint32_t*>(reinterpret_cast<const float*>(r.h_state + 6 * n) + 4 * n);
   const uint32_t bits = herr[0] | herr[1];
-  if (h_out && h_out->count == n) {
+  if (h_out && h_out->count >= n) {
     const double* d = r.h_state;
     float* dst[6] = {h_out->pos_x, h_out->pos_y, h_out->pos_z, h_out->vel_x, h_out->vel_y, h_out->vel_z};
     for (int k = 0; k < 6; ++k)
@@ -941,7 +933,6 @@ nbgb_status nbgb_ensemble_poll(nbgb_ensemble* e, nbgb_ensemble_result* result,
   if (state_f64) std::copy(r.h_state, r.h_state + 6 * n, state_f64);
   cudaFreeHost(r.h_state);
   cudaEventDestroy(r.evt);
-  if (r.sys) release_system(*r.sys);
   e->retiring.pop_front();
   if (bits) {
     g_ens_err = "device error word set during the ensemble run";
@@ -965,12 +956,17 @@ nbgb_status nbgb_ensemble_get_stream(nbgb_ensemble* e, void** cuda_stream) {
 
 nbgb_status nbgb_ensemble_get_stats(nbgb_ensemble* e, nbgb_ensemble_stats* s) {
   if (!e || !s) return NBGB_ERR_INVALID_ARG;
+  unsigned long long bh_inter = 0;
   try {
     harvest_all(e);
+    NBGB_CUDA(cudaMemcpyAsync(&bh_inter, e->d_bh_inter.ptr, sizeof bh_inter,
+                              cudaMemcpyDeviceToHost, e->main));
+    NBGB_CUDA(cudaStreamSynchronize(e->main));
   } catch (const Error& err) {
     return err.status;
   }
   *s = e->st;
+  s->bh_interactions = (double)bh_inter;
   s->direct_kernel_ms = e->dk_ms;
   s->direct_kernel_interactions = e->dk_inter;
   s->resident = (int32_t)e->resident.size();

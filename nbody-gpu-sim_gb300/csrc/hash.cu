@@ -217,7 +217,7 @@ void hash_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, flo
   uint32_t* sws = h.scan_ws.ensure(scan_workspace_elems((int64_t)radix_hist_elems(n)) +
                                    scan_workspace_elems(total + 1));
   radix_sort_pairs<uint32_t>(keys, keys_alt, vals, vals_alt, n, 0, end_bit, hist, sws, st,
-                             &h.in_alt);
+                             &h.in_alt, c->err.ensure(1));
   // 4. cell starts
   uint32_t* start = h.cell_start.ensure((size_t)total + 1);
   hash_cell_start_kernel<<<grid1d(total + 1), 256, 0, st>>>(h.sorted_cells(), n, total, start);

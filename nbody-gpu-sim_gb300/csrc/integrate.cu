@@ -86,11 +86,12 @@ void launch_store_old(const nbgb_particle_data& d, cudaStream_t st) {
   NBGB_LAUNCH_CHECK();
 }
 
+template <typename A>
 __global__ void kick_drift_kernel(int64_t n, double* __restrict__ x, double* __restrict__ y,
                                   double* __restrict__ z, double* __restrict__ vx,
                                   double* __restrict__ vy, double* __restrict__ vz,
-                                  const float* __restrict__ ax, const float* __restrict__ ay,
-                                  const float* __restrict__ az, double kick, double dt,
+                                  const A* __restrict__ ax, const A* __restrict__ ay,
+                                  const A* __restrict__ az, double kick, double dt,
                                   float4* __restrict__ pm) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -114,10 +115,10 @@ __global__ void kick_drift_kernel(int64_t n, double* __restrict__ x, double* __r
   }
 }
 
+template <typename A>
 __global__ void kick_kernel(int64_t n, double* __restrict__ vx, double* __restrict__ vy,
-                            double* __restrict__ vz, const float* __restrict__ ax,
-                            const float* __restrict__ ay, const float* __restrict__ az,
-                            double kick) {
+                            double* __restrict__ vz, const A* __restrict__ ax,
+                            const A* __restrict__ ay, const A* __restrict__ az, double kick) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     vx[i] = fma((double)ax[i], kick, vx[i]);
@@ -126,20 +127,41 @@ __global__ void kick_kernel(int64_t n, double* __restrict__ vx, double* __restri
   }
 }
 
-void launch_kick_drift(int64_t n, double* x, double* y, double* z, double* vx, double* vy,
-                       double* vz, const float* ax, const float* ay, const float* az,
-                       double kick, double dt, float4* pm, cudaStream_t st) {
+template <typename A>
+static void kick_drift_any(int64_t n, double* x, double* y, double* z, double* vx, double* vy,
+                           double* vz, const A* ax, const A* ay, const A* az, double kick,
+                           double dt, float4* pm, cudaStream_t st) {
   if (n <= 0) return;
-  kick_drift_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, x, y, z, vx, vy, vz, ax, ay, az, kick,
-                                                      dt, pm);
+  kick_drift_kernel<A><<<grid_for(n, 256), 256, 0, st>>>(n, x, y, z, vx, vy, vz, ax, ay, az, kick,
+                                                         dt, pm);
   NBGB_LAUNCH_CHECK();
 }
 
+template <typename A>
+static void kick_any(int64_t n, double* vx, double* vy, double* vz, const A* ax, const A* ay,
+                     const A* az, double kick, cudaStream_t st) {
+  if (n <= 0) return;
+  kick_kernel<A><<<grid_for(n, 256), 256, 0, st>>>(n, vx, vy, vz, ax, ay, az, kick);
+  NBGB_LAUNCH_CHECK();
+}
+
+void launch_kick_drift(int64_t n, double* x, double* y, double* z, double* vx, double* vy,
+                       double* vz, const float* ax, const float* ay, const float* az,
+                       double kick, double dt, float4* pm, cudaStream_t st) {
+  kick_drift_any(n, x, y, z, vx, vy, vz, ax, ay, az, kick, dt, pm, st);
+}
+void launch_kick_drift(int64_t n, double* x, double* y, double* z, double* vx, double* vy,
+                       double* vz, const double* ax, const double* ay, const double* az,
+                       double kick, double dt, float4* pm, cudaStream_t st) {
+  kick_drift_any(n, x, y, z, vx, vy, vz, ax, ay, az, kick, dt, pm, st);
+}
 void launch_kick(int64_t n, double* vx, double* vy, double* vz, const float* ax, const float* ay,
                  const float* az, double kick, cudaStream_t st) {
-  if (n <= 0) return;
-  kick_kernel<<<grid_for(n, 256), 256, 0, st>>>(n, vx, vy, vz, ax, ay, az, kick);
-  NBGB_LAUNCH_CHECK();
+  kick_any(n, vx, vy, vz, ax, ay, az, kick, st);
+}
+void launch_kick(int64_t n, double* vx, double* vy, double* vz, const double* ax,
+                 const double* ay, const double* az, double kick, cudaStream_t st) {
+  kick_any(n, vx, vy, vz, ax, ay, az, kick, st);
 }
 
 }  // namespace nbgb

@@ -77,5 +77,19 @@ void launch_kick_drift(int64_t n, double* x, double* y, double* z, double* vx, d
 // FP64-state kick: v += a*kick.
 void launch_kick(int64_t n, double* vx, double* vy, double* vz, const float* ax,
                  const float* ay, const float* az, double kick, cudaStream_t st);
+// The same with FP64 accelerations (full-FP64 system).
+void launch_kick_drift(int64_t n, double* x, double* y, double* z, double* vx, double* vy,
+                       double* vz, const double* ax, const double* ay, const double* az,
+                       double kick, double dt, float4* pm, cudaStream_t st);
+void launch_kick(int64_t n, double* vx, double* vy, double* vz, const double* ax,
+                 const double* ay, const double* az, double kick, cudaStream_t st);
+// Direct forces and potential energy in FP64 from FP64 positions (masses
+// from pm.w).
+void launch_direct_f64_state(const double* x, const double* y, const double* z, const float4* pm,
+                             int64_t n, double G, double eps2, double* ax, double* ay, double* az,
+                             cudaStream_t st);
+void launch_potential_f64(const double* x, const double* y, const double* z, const float4* pm,
+                          int64_t n, double eps2, double* partials, int nblocks, double* out,
+                          cudaStream_t st);
 
 }  // namespace nbgb

@@ -6,12 +6,18 @@
 // radix sort produces for primitive keys, so (key, value) outputs compare
 // bit-exactly with the reference.
 //
-// Radix pass (8-bit digit, tiles of kSortTile items):
-//   1. digit histogram per tile -> hist[digit * n_tiles + tile]
-//   2. exclusive scan of hist (digit-major) -> global offset per (digit, tile)
-//   3. scatter: each tile ranks its items stably (warp match + per-warp digit
-//      counts in shared memory, rounds in input order) and writes them to
-//      offset + rank.
+// Radix sort (8-bit digits, tiles of 4096 items), one kernel per digit:
+//   0. one histogram kernel reads the keys once and counts every digit of
+//      every pass; its last block turns the counts into each pass's global
+//      digit offsets;
+//   1. per pass, each CTA takes the next tile (dynamic tile id), ranks its
+//      items stably (warp match + per-warp digit counts over rounds in input
+//      order), publishes its per-digit counts, obtains the counts of all
+//      earlier tiles by decoupled look-back over their published
+//      aggregates / inclusive prefixes (every wait bounded), sorts the tile
+//      by digit in shared memory and writes it out in digit runs (coalesced).
+// Inputs of 2^30 items or more use the three-phase path (per-tile
+// histograms, device-wide scan, scatter), 5 launches per pass.
 #include "common.cuh"
 #include "kernels.cuh"
 #include "sort.cuh"
@@ -205,9 +211,9 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
 }
 
 template <typename K>
-void radix_sort_pairs(K* keys, K* keys_alt, uint32_t* vals, uint32_t* vals_alt, int64_t n,
-                      int begin_bit, int end_bit, uint32_t* hist, uint32_t* scan_ws,
-                      cudaStream_t st, bool* result_in_alt) {
+static void radix_sort_pairs_3phase(K* keys, K* keys_alt, uint32_t* vals, uint32_t* vals_alt,
+                                    int64_t n, int begin_bit, int end_bit, uint32_t* hist,
+                                    uint32_t* scan_ws, cudaStream_t st, bool* result_in_alt) {
   *result_in_alt = false;
   if (n <= 1) return;
   const int64_t n_tiles = ceil_div(n, kSortTile);
@@ -231,12 +237,234 @@ void radix_sort_pairs(K* keys, K* keys_alt, uint32_t* vals, uint32_t* vals_alt, 
   *result_in_alt = alt;
 }
 
-size_t radix_hist_elems(int64_t n) { return (size_t)256 * ceil_div(std::max<int64_t>(n, 1), kSortTile); }
+// ------------------------------------------------- one-sweep radix sort --
+constexpr int kOSThreads = 256;
+constexpr int kOSItems = 16;
+constexpr int kOSTile = kOSThreads * kOSItems;  // == kSortTile
+constexpr int kOSWarps = kOSThreads / 32;
+constexpr int kOSWarpItems = kOSTile / kOSWarps;  // consecutive items per warp
+constexpr int kOSMaxPasses = 8;
+constexpr uint32_t kOSValMask = (1u << 30) - 1u;
+constexpr uint32_t kOSAgg = 1u << 30;  // tile aggregate published
+constexpr uint32_t kOSInc = 2u << 30;  // inclusive prefix published
+constexpr uint32_t kOSSpinLimit = 1u << 22;
+// workspace (u32): counts [8][256] | offsets [8][256] | tile counters [8],
+// ticket | status [passes][n_tiles][256]
+constexpr int kOSCounters = 2 * kOSMaxPasses * 256;
+constexpr int kOSHeader = kOSCounters + 256;
+constexpr int64_t kOSMaxItems = (int64_t)1 << 30;  // prefixes fit 30 bits
+
+__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Exclusive scan of one value per thread over a 256-thread block.
+__device__ __forceinline__ uint32_t block_excl_scan256(uint32_t v, uint32_t* s_w) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) s_w[warp] = x;
+  __syncthreads();
+  uint32_t wp = 0;
+  for (int w = 0; w < warp; ++w) wp += s_w[w];
+  __syncthreads();
+  return wp + x - v;
+}
+
+template <typename K>
+__global__ void __launch_bounds__(256) onesweep_hist_kernel(const K* __restrict__ keys, int64_t n,
+                                                            int begin_bit, int passes,
+                                                            uint32_t* __restrict__ ws) {
+  __shared__ uint32_t s_h[kOSMaxPasses][256];
+  __shared__ uint32_t s_w[8];
+  __shared__ bool s_last;
+  for (int e = threadIdx.x; e < kOSMaxPasses * 256; e += blockDim.x) (&s_h[0][0])[e] = 0;
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const K k = keys[i];
+    for (int p = 0; p < passes; ++p) atomicAdd(&s_h[p][digit_of(k, begin_bit + 8 * p)], 1u);
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < passes * 256; e += blockDim.x) {
+    const uint32_t c = (&s_h[0][0])[e];
+    if (c) atomicAdd(&ws[e], c);
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&ws[kOSCounters + kOSMaxPasses], 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  for (int p = 0; p < passes; ++p) {  // last block: digit offsets of every pass
+    const uint32_t c = __ldcg(&ws[p * 256 + threadIdx.x]);
+    const uint32_t e = block_excl_scan256(c, s_w);
+    ws[kOSMaxPasses * 256 + p * 256 + threadIdx.x] = e;
+  }
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kOSThreads) onesweep_pass_kernel(
+    const K* __restrict__ kin, const uint32_t* __restrict__ vin, K* __restrict__ kout,
+    uint32_t* __restrict__ vout, int64_t n, int shift, int pass, int64_t n_tiles,
+    uint32_t* __restrict__ ws, uint32_t* err) {
+  extern __shared__ __align__(16) unsigned char os_smem[];
+  K* s_keys = reinterpret_cast<K*>(os_smem);                          // [kOSTile]
+  uint32_t* s_vals = reinterpret_cast<uint32_t*>(s_keys + kOSTile);   // [kOSTile]
+  uint32_t* s_wh = s_vals + kOSTile;                                  // [kOSWarps][256]
+  uint32_t* s_loc = s_wh + kOSWarps * 256;                            // [256]
+  long long* s_gb = reinterpret_cast<long long*>(s_loc + 256);        // [256]
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_w[kOSWarps];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(&ws[kOSCounters + pass], 1u);
+  for (int e = tid; e < kOSWarps * 256; e += kOSThreads) s_wh[e] = 0;
+  __syncthreads();
+  const int64_t tile = s_tile;
+  const int64_t wbase = tile * kOSTile + (int64_t)warp * kOSWarpItems;
+  K key[kOSItems];
+  uint32_t rank[kOSItems];
+#pragma unroll
+  for (int r = 0; r < kOSItems; ++r) {
+    const int64_t i = wbase + r * 32 + lane;
+    key[r] = (i < n) ? kin[i] : (K)0;
+  }
+  // stable rank within the warp's 512 consecutive items
+  uint32_t* wh = s_wh + warp * 256;
+  const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+  for (int r = 0; r < kOSItems; ++r) {
+    const bool valid = wbase + r * 32 + lane < n;
+    const uint32_t d = valid ? digit_of(key[r], shift) : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    uint32_t old = 0;
+    if (valid && lane == leader) {
+      old = wh[d];
+      wh[d] = old + __popc(peers);
+    }
+    old = __shfl_sync(0xffffffffu, old, leader);
+    rank[r] = old + __popc(peers & lt);
+    __syncwarp();
+  }
+  __syncthreads();
+  // per digit (thread d): offsets of each warp, tile total, publication
+  const int d = tid;
+  uint32_t total = 0;
+  for (int w = 0; w < kOSWarps; ++w) {
+    const uint32_t c = s_wh[w * 256 + d];
+    s_wh[w * 256 + d] = total;
+    total += c;
+  }
+  uint32_t* status = ws + kOSHeader + ((int64_t)pass * n_tiles) * 256;
+  st_relaxed_u32(&status[tile * 256 + d], (tile == 0 ? kOSInc : kOSAgg) | total);
+  s_loc[d] = block_excl_scan256(total, s_w);
+  // decoupled look-back over earlier tiles (bounded waits)
+  uint32_t excl = 0;
+  if (tile > 0) {
+    for (int64_t t = tile - 1; t >= 0; --t) {
+      const uint32_t* sp = &status[t * 256 + d];
+      uint32_t sv = ld_relaxed_u32(sp);
+      uint32_t spins = 0;
+      while ((sv & ~kOSValMask) == 0u && ++spins < kOSSpinLimit) {
+        if (spins > 32) __nanosleep(64);
+        sv = ld_relaxed_u32(sp);
+      }
+      if ((sv & ~kOSValMask) == 0u) {
+        raise_error(err, kErrWaitTimeout);
+        break;
+      }
+      excl += sv & kOSValMask;
+      if ((sv & ~kOSValMask) == kOSInc) break;
+    }
+    st_relaxed_u32(&status[tile * 256 + d], kOSInc | ((excl + total) & kOSValMask));
+  }
+  s_gb[d] = (long long)ws[kOSMaxPasses * 256 + pass * 256 + d] + excl - s_loc[d];
+  __syncthreads();
+  // local sort by digit in shared memory
+#pragma unroll
+  for (int r = 0; r < kOSItems; ++r) {
+    const int64_t i = wbase + r * 32 + lane;
+    if (i < n) {
+      const uint32_t dd = digit_of(key[r], shift);
+      const uint32_t li = s_loc[dd] + s_wh[warp * 256 + dd] + rank[r];
+      s_keys[li] = key[r];
+      s_vals[li] = vin[i];
+    }
+  }
+  __syncthreads();
+  // digit runs out to their global positions
+  const int cnt = (int)imin64(kOSTile, n - tile * kOSTile);
+  for (int j = tid; j < cnt; j += kOSThreads) {
+    const K k = s_keys[j];
+    const long long pos = s_gb[digit_of(k, shift)] + j;
+    kout[pos] = k;
+    vout[pos] = s_vals[j];
+  }
+}
+
+template <typename K>
+static size_t onesweep_smem() {
+  return (size_t)kOSTile * (sizeof(K) + 4) + (size_t)kOSWarps * 256 * 4 + 256 * 4 + 256 * 8;
+}
+
+template <typename K>
+void radix_sort_pairs(K* keys, K* keys_alt, uint32_t* vals, uint32_t* vals_alt, int64_t n,
+                      int begin_bit, int end_bit, uint32_t* hist, uint32_t* scan_ws,
+                      cudaStream_t st, bool* result_in_alt, uint32_t* err) {
+  *result_in_alt = false;
+  if (n <= 1) return;
+  if (n >= kOSMaxItems) {
+    radix_sort_pairs_3phase(keys, keys_alt, vals, vals_alt, n, begin_bit, end_bit, hist, scan_ws,
+                            st, result_in_alt);
+    return;
+  }
+  const int passes = (end_bit - begin_bit + 7) / 8;
+  const int64_t n_tiles = ceil_div(n, kOSTile);
+  uint32_t* ws = hist;
+  NBGB_CUDA(cudaMemsetAsync(ws, 0, ((size_t)kOSHeader + (size_t)passes * n_tiles * 256) * 4, st));
+  const unsigned hb = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 4096), num_sms() * 4));
+  onesweep_hist_kernel<K><<<hb, 256, 0, st>>>(keys, n, begin_bit, passes, ws);
+  NBGB_LAUNCH_CHECK();
+  const size_t smem = onesweep_smem<K>();
+  NBGB_CUDA(cudaFuncSetAttribute(onesweep_pass_kernel<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+  K* kin = keys;
+  K* kout = keys_alt;
+  uint32_t* vin = vals;
+  uint32_t* vout = vals_alt;
+  bool alt = false;
+  for (int p = 0; p < passes; ++p) {
+    onesweep_pass_kernel<K><<<(unsigned)n_tiles, kOSThreads, smem, st>>>(
+        kin, vin, kout, vout, n, begin_bit + 8 * p, p, n_tiles, ws, err);
+    NBGB_LAUNCH_CHECK();
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+    alt = !alt;
+  }
+  *result_in_alt = alt;
+}
+
+size_t radix_hist_elems(int64_t n) {
+  const int64_t tiles = ceil_div(std::max<int64_t>(n, 1), kSortTile);
+  return (size_t)kOSHeader + (size_t)kOSMaxPasses * 256 * tiles;  // covers the 3-phase layout too
+}
 
 template void radix_sort_pairs<uint32_t>(uint32_t*, uint32_t*, uint32_t*, uint32_t*, int64_t, int,
-                                         int, uint32_t*, uint32_t*, cudaStream_t, bool*);
+                                         int, uint32_t*, uint32_t*, cudaStream_t, bool*,
+                                         uint32_t*);
 template void radix_sort_pairs<unsigned long long>(unsigned long long*, unsigned long long*,
                                                    uint32_t*, uint32_t*, int64_t, int, int,
-                                                   uint32_t*, uint32_t*, cudaStream_t, bool*);
+                                                   uint32_t*, uint32_t*, cudaStream_t, bool*,
+                                                   uint32_t*);
 
 }  // namespace nbgb

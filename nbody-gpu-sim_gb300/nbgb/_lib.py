@@ -62,6 +62,7 @@ assert C.sizeof(ParticleDataStruct) == 13 * 8 + 8
 FLAG_SYNC = 0x1
 FLAG_COMPENSATED = 0x2
 FLAG_COUNT_INTERACTIONS = 0x4
+FLAG_FP64 = 0x8
 
 _vp = C.c_void_p
 _i32p = C.POINTER(C.c_int32)

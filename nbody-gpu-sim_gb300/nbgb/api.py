@@ -14,7 +14,8 @@ from enum import IntEnum
 import numpy as np
 
 from . import _lib
-from ._lib import FLAG_COMPENSATED, FLAG_COUNT_INTERACTIONS, FLAG_SYNC, OctreeNode, Params
+from ._lib import (FLAG_COMPENSATED, FLAG_COUNT_INTERACTIONS, FLAG_FP64, FLAG_SYNC, OctreeNode,
+                   Params)
 from ._lib import ParticleDataStruct
 
 FIELDS = ("pos_x", "pos_y", "pos_z", "vel_x", "vel_y", "vel_z", "acc_x", "acc_y", "acc_z",
@@ -452,4 +453,5 @@ __all__ = ["ForceMethod", "forceMethodToString", "ParticleData", "ParticleDataMa
            "BarnesHutCalculator", "SpatialHashCalculator", "createForceCalculator",
            "Integrator", "System", "ValidationException", "ResourceException", "CudaException",
            "DeviceTimeout", "CapacityError", "NbodyError", "check", "default_params",
-           "FLAG_SYNC", "FLAG_COMPENSATED", "FLAG_COUNT_INTERACTIONS", "OctreeNode", "Params"]
+           "FLAG_SYNC", "FLAG_COMPENSATED", "FLAG_COUNT_INTERACTIONS", "FLAG_FP64", "OctreeNode",
+           "Params"]

@@ -51,25 +51,39 @@ class Ensemble:
         check(_lib.lib().nbgb_ensemble_tick(self.handle, C.byref(r), C.byref(q)))
         return r.value, q.value
 
-    def poll(self, want_state: bool = False):
-        """Next finished request as (result dict, FP64 state dict or None),
-        or None when nothing has finished."""
+    def poll(self, want_state: bool = False, want_acc: bool = False):
+        """Next finished request as (result dict, state dict or None), or None
+        when nothing has finished.  The state holds the FP64 x..vz
+        (want_state) and the FP32 ax, ay, az, m at the final positions
+        (want_acc)."""
         res = EnsembleResult()
         f64 = None
-        if want_state and self.sizes:
+        cap = max(self.sizes.values()) if self.sizes else 0
+        if want_state and cap:
             # large enough for whichever request finishes next
-            f64 = np.zeros(6 * max(self.sizes.values()), np.float64)
-        st = _lib.lib().nbgb_ensemble_poll(self.handle, C.byref(res), None,
+            f64 = np.zeros(6 * cap, np.float64)
+        hout, facc = None, None
+        if want_acc and cap:
+            facc = np.zeros((4, cap), np.float32)
+            hout = _lib.ParticleDataStruct()
+            hout.acc_x, hout.acc_y, hout.acc_z, hout.mass = (facc[i].ctypes.data for i in range(4))
+            hout.count = cap
+        st = _lib.lib().nbgb_ensemble_poll(self.handle, C.byref(res),
+                                            None if hout is None else C.byref(hout),
                                             None if f64 is None else f64.ctypes.data)
         if st == NOT_READY:
             return None
         check(st)
         self.sizes.pop(res.request_id, None)
         state = None
+        n = res.count
+        if f64 is not None or facc is not None:
+            state = {}
         if f64 is not None:
-            n = res.count
             keys = ("x", "y", "z", "vx", "vy", "vz")
-            state = {k: f64[i * n:(i + 1) * n].copy() for i, k in enumerate(keys)}
+            state.update({k: f64[i * n:(i + 1) * n].copy() for i, k in enumerate(keys)})
+        if facc is not None:
+            state.update({k: facc[i, :n].copy() for i, k in enumerate(("ax", "ay", "az", "m"))})
         return _res(res), state
 
     def synchronize(self) -> None:

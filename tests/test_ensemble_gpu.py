@@ -151,3 +151,46 @@ def test_autotuner_settles(nb):
     assert st["tuning"] == 0 and 0 <= st["direct_config"] < 6
     assert st["direct_kernel_ms"] > 0 and st["direct_kernel_interactions"] > 0
     ens.close()
+
+
+def test_batched_bh_bitwise_vs_calculator(nb):
+    """Barnes-Hut systems of uneven N (one body, two bodies, ragged tails of
+    the 32-target warp tasks, two clusters) share one batched build + walk;
+    each system's final acceleration equals the single-system calculator's
+    on the same FP32 positions bit for bit."""
+    from nbgb.serving import Ensemble
+    sizes = (1, 2, 33, 1500, 4097, 12000)
+    ens = Ensemble(direct_max_n=0, hbm_budget_bytes=2 << 30)
+    reqs = {}
+    for i, n in enumerate(sizes):
+        s = nb.ics.plummer(n, seed=70 + i) if n != 4097 else nb.ics.two_plummer(n, seed=70 + i)
+        reqs[ens.submit(s, 3 + i, 1e-3)] = n
+    got = {}
+    for _ in range(100):
+        if ens.tick() == (0, 0):
+            break
+    ens.synchronize()
+    while (r := ens.poll(want_state=True, want_acc=True)) is not None:
+        got[r[0]["request_id"]] = r[1]
+    st = ens.stats()
+    ens.close()
+    assert len(got) == len(reqs)
+    assert st["bh_interactions"] > 0 and st["direct_interactions"] == 0
+    for rid, s in got.items():
+        pos = {k: s[k].astype(np.float32) for k in ("x", "y", "z")}
+        ref = _calc_bh(nb, pos, s["m"])
+        for k, a in zip(("ax", "ay", "az"), ref):
+            np.testing.assert_array_equal(s[k], a, err_msg=f"n={reqs[rid]} {k}")
+
+
+def _calc_bh(nb, pos, m, theta=0.5, eps=0.01):
+    calc = nb.BarnesHutCalculator(theta)
+    calc.setSofteningParameter(eps)
+    n = len(m)
+    with nb.ScopedParticleData(n, {"pos_x": pos["x"], "pos_y": pos["y"], "pos_z": pos["z"],
+                                   "mass": m}) as p:
+        calc.computeForces(p.device)
+        p.download()
+        acc = (p.host["acc_x"].copy(), p.host["acc_y"].copy(), p.host["acc_z"].copy())
+    calc.close()
+    return acc

@@ -156,3 +156,40 @@ def test_system_trajectory_vs_fp64(nb, orc):
     assert dv <= 2e-4, dv
     e0, e1 = ke0 + pe0, ke1 + pe1
     assert abs(e1 - e0) / abs(e0) <= 1e-5
+
+
+def test_system_full_fp64_vs_oracle(nb, orc):
+    """NBGB_FLAG_FP64: FP64 forces from the FP64 state.  Trajectory within
+    1e-10 of the FP64 oracle after 100 steps (the two differ only in
+    summation order and the library rsqrt), energy within 1e-12 relative."""
+    n, eps, dt, steps = _c1()
+    s = nb.ics.plummer(n, seed=1)
+    calc = nb.DirectForceCalculator()
+    calc.setSofteningParameter(eps)
+    calc.set_flags(nb.FLAG_SYNC | nb.FLAG_FP64)
+    sysm = nb.System(calc, s)
+    ke0, pe0, _ = sysm.energy()
+    sysm.step(dt, steps)
+    got = sysm.read_f64()
+    sysm.close()
+    calc.close()
+    st = {k: s[k].astype(np.float64) for k in ("x", "y", "z", "vx", "vy", "vz")}
+    m = s["m"].astype(np.float64)
+    pe_ref = orc.potential_energy(st["x"], st["y"], st["z"], m, 1.0, eps)
+    assert abs(pe0 - pe_ref) <= 1e-12 * abs(pe_ref)
+    st["ax"], st["ay"], st["az"] = orc.direct_f64(st["x"], st["y"], st["z"], m, 1.0, eps)
+    for _ in range(steps):
+        orc.vv_step_f64(st, m, 1.0, eps, dt)
+    dx = max(np.abs(got[k] - st[k]).max() for k in ("x", "y", "z"))
+    dv = max(np.abs(got[k] - st[k]).max() for k in ("vx", "vy", "vz"))
+    assert dx <= 1e-10, dx
+    assert dv <= 1e-9, dv
+
+
+def test_fp64_flag_requires_direct(nb):
+    s = nb.ics.plummer(256, seed=2)
+    calc = nb.BarnesHutCalculator(0.5)
+    calc.set_flags(nb.FLAG_SYNC | nb.FLAG_FP64)
+    with pytest.raises(nb.ValidationException):
+        nb.System(calc, s)
+    calc.close()
