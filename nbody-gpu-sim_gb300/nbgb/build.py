@@ -18,6 +18,8 @@ CSRC = os.path.join(ROOT, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 BUILD_DIR = os.path.join(ROOT, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libnbgb.so")
+APP_SRC = os.path.join(ROOT, "app", "nbgb_sim.cpp")
+APP_PATH = os.path.join(PKG_DIR, "nbgb_sim")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
@@ -52,9 +54,30 @@ def is_stale() -> bool:
     return any(os.path.getmtime(p) > t for p in sources() + _headers() + [__file__])
 
 
+def build_app(force: bool = False) -> str:
+    """The headless driver ``nbgb_sim`` (host C++ over libnbgb.so, rpath to
+    its own directory); FP contraction off so its initial conditions are
+    evaluated like the reference's host code."""
+    if (not force and os.path.exists(APP_PATH) and
+            os.path.getmtime(APP_PATH) >= max(os.path.getmtime(APP_SRC), os.path.getmtime(LIB_PATH),
+                                              os.path.getmtime(os.path.join(INCLUDE, "nbgb.h")))):
+        return APP_PATH
+    cxx = os.environ.get("CXX", "g++")
+    tmp = APP_PATH + ".tmp"
+    r = subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-Wall", "-I", INCLUDE, APP_SRC,
+                        "-o", tmp, "-L", PKG_DIR, "-lnbgb", "-Wl,-rpath,$ORIGIN"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed for nbgb_sim:\n" + r.stdout + r.stderr)
+    os.replace(tmp, APP_PATH)
+    return APP_PATH
+
+
 def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> str:
-    """Compile and link libnbgb.so; returns its path."""
+    """Compile and link libnbgb.so (and the nbgb_sim driver); returns the
+    library path."""
     if not force and not is_stale():
+        build_app()
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     nvcc = _nvcc()
@@ -71,8 +94,9 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     tmp = LIB_PATH + ".tmp"
     _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs)
     os.replace(tmp, LIB_PATH)
+    build_app(force=True)
     if verbose:
-        print("built", LIB_PATH)
+        print("built", LIB_PATH, "and", APP_PATH)
     return LIB_PATH
 
 

@@ -204,3 +204,4 @@ def test_full_size_two_plummer(nb, orc):
     r8 = _bh(nb, s, theta=0.5, leaf=8, count=False)
     err8 = vec_rel_err(*(a[t] for a in r8["acc"]), bx, by, bz)
     assert np.median(err8) <= 2e-3
+

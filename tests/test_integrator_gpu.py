@@ -175,6 +175,8 @@ def test_system_full_fp64_vs_oracle(nb, orc):
     calc.close()
     st = {k: s[k].astype(np.float64) for k in ("x", "y", "z", "vx", "vy", "vz")}
     m = s["m"].astype(np.float64)
+    eps = float(np.float32(eps))  # the calculator holds softening as a float
+    dt = float(np.float32(dt))
     pe_ref = orc.potential_energy(st["x"], st["y"], st["z"], m, 1.0, eps)
     assert abs(pe0 - pe_ref) <= 1e-12 * abs(pe_ref)
     st["ax"], st["ay"], st["az"] = orc.direct_f64(st["x"], st["y"], st["z"], m, 1.0, eps)
