@@ -59,6 +59,15 @@ using u64 = unsigned long long;
 constexpr int kHiLevels = 21;  // levels 1..21 in the high key (63 bits)
 constexpr int kMaxDepth = 32;  // force_barnes_hut.cu:24
 
+// One octree node, 64 bytes (one walk visit touches one 64-byte block).
+struct __align__(16) Node {
+  float4 com;   // centre of mass, total mass
+  float4 geom;  // cube centre, half size
+  int4 info;    // skip (next node outside the subtree), first body, body count,
+                // depth << 8 | leaf
+  float4 pad;
+};
+
 struct BHState {
   // segment tables (device; single-system calls fill one segment)
   DevBuf<char> tables;           // seg_off [nseg], seg_base [nseg + 1], tasks [ntasks]
@@ -83,11 +92,11 @@ struct BHState {
   DevBuf<uint32_t> nstart;  // n + 1
   DevBuf<uint32_t> scalars; // [0] total nodes
   HostPinned<uint32_t> h_scalars;
-  DevBuf<float4> node_com, node_geom;
-  DevBuf<int4> node_info;  // skip, first, count, flags (bit0 leaf, bits 8.. depth)
+  DevBuf<Node> nodes;
   DevBuf<int32_t> node_parent, node_nchild, node_visit;
   DevBuf<float4> spm;      // bodies in path order
   DevBuf<unsigned long long> inter_total;
+  DevBuf<uint32_t> walk_ctr;  // next warp task of the walk
   int64_t n = 0;
   int64_t reserve = 0;  // bodies the per-body buffers are sized for (>= n)
   int64_t cap = 0;      // node capacity
@@ -445,8 +454,7 @@ struct EmitArgs {
   const int64_t* base;  // segment s occupies sorted positions [base[s], base[s+1])
   int64_t n;
   int64_t cap;
-  float4* geom;
-  int4* info;
+  Node* nodes;
   int32_t* parent;
   int32_t* visit;
   int32_t* seg_root;
@@ -476,57 +484,93 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
     if (first) {
       const int64_t send = a.base[s + 1];  // one past the segment's last position
       const uint32_t skip = (send < a.n) ? a.nstart[send] : total;
-      a.geom[idx] = make_float4(b.center[0], b.center[1], b.center[2], b.half);
-      a.info[idx] = make_int4((int)skip, (int)k, (int)(send - k), 0);
+      a.nodes[idx].geom = make_float4(b.center[0], b.center[1], b.center[2], b.half);
+      a.nodes[idx].info = make_int4((int)skip, (int)k, (int)(send - k), 0);
       a.parent[idx] = -1;
       a.visit[idx] = 0;
       a.seg_root[s] = (int32_t)idx;
       a.seg_end[s] = (int32_t)skip;
       ++idx;
     }
-    // walk the path of body k once, emitting internal nodes of depth fd..top
-    float cx = b.center[0], cy = b.center[1], cz = b.center[2], h = b.half;
+    // internal nodes of depth fd..top: slots claimed here (owner = k in
+    // parent[]), filled by internal_nodes_kernel, one thread per node
+    const int n_int = max(0, top - fd + 1);
+    for (int j = 0; j < n_int; ++j) a.parent[idx + j] = (int32_t)k;
+    idx += n_int;
     const bool leaf_start = first || (lp < kMaxDepth);
-    const int ld = min(kMaxDepth, max(lp, lk) + 1);
-    const int lastlev = leaf_start ? ld : top;
-    for (int lev = 1; lev <= lastlev; ++lev) {
+    int md = -1;
+    if (leaf_start) {
+      const int ld = min(kMaxDepth, max(lp, lk) + 1);
+      float cx = b.center[0], cy = b.center[1], cz = b.center[2], h = b.half;
+      for (int lev = 1; lev <= ld; ++lev) {
+        const uint32_t o = (p.x >= cx ? 1u : 0u) | (p.y >= cy ? 2u : 0u) | (p.z >= cz ? 4u : 0u);
+        const float hs = __fmul_rn(h, 0.5f);
+        cx = __fadd_rn(cx, (o & 1u) ? hs : -hs);
+        cy = __fadd_rn(cy, (o & 2u) ? hs : -hs);
+        cz = __fadd_rn(cz, (o & 4u) ? hs : -hs);
+        h = hs;
+      }
+      int64_t e = k;
+      while (e + 1 < a.n && a.kseg[e + 1] == s && (int)a.lcp[e] >= kMaxDepth) ++e;
+      a.nodes[idx].geom = make_float4(cx, cy, cz, h);
+      a.nodes[idx].info = make_int4((int)(idx + 1), (int)k, (int)(e - k + 1), (ld << 8) | 1);
+      a.parent[idx] = -1;
+      a.visit[idx] = 0;
+      // reference max_depth_: depth of the inserting body's last loop level
+      md = (ld == kMaxDepth && e > k) ? kMaxDepth : ld - 1;
+    }
+    // per-segment maximum: reduced over the lanes of the same segment, one
+    // atomic per group and only while it can still raise the stored value
+    const unsigned peers = __match_any_sync(__activemask(), s);
+    const int gmax = __reduce_max_sync(peers, md);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1 && gmax > __ldcg(&a.seg_depth[s]))
+      atomicMax(&a.seg_depth[s], gmax);
+  }
+}
+
+// Internal nodes, one thread per node: the owner body k (the first body of
+// the node's range) and the depth follow from k's slot numbering; the centre
+// is k's path to that depth, the range end a search over the sorted keys.
+__global__ void internal_nodes_kernel(EmitArgs a) {
+  const uint32_t total = a.nstart[a.n];
+  if ((int64_t)total > a.cap) return;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < (int64_t)total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t k32 = a.parent[q];
+    if (k32 < 0) continue;  // a root or a leaf
+    const int64_t k = k32;
+    const int32_t s = a.kseg[k];
+    const bool first = (k == 0) || a.kseg[k - 1] != s;
+    const int fd = first ? 1 : (int)a.lcp[k - 1] + 1;
+    const int d = fd + (int)(q - (int64_t)a.nstart[k]) - (first ? 1 : 0);
+    const float4 p = a.spm[k];
+    const BBox b = a.box[s];
+    float cx = b.center[0], cy = b.center[1], cz = b.center[2], h = b.half;
+    for (int lev = 1; lev <= d; ++lev) {
       const uint32_t o = (p.x >= cx ? 1u : 0u) | (p.y >= cy ? 2u : 0u) | (p.z >= cz ? 4u : 0u);
       const float hs = __fmul_rn(h, 0.5f);
       cx = __fadd_rn(cx, (o & 1u) ? hs : -hs);
       cy = __fadd_rn(cy, (o & 2u) ? hs : -hs);
       cz = __fadd_rn(cz, (o & 4u) ? hs : -hs);
       h = hs;
-      if (lev >= fd && lev <= top) {
-        const int64_t e = range_end(a.kseg, a.hi, a.lo, a.n, k, lev);
-        const uint32_t skip = (e + 1 < a.n) ? a.nstart[e + 1] : total;
-        a.geom[idx] = make_float4(cx, cy, cz, h);
-        a.info[idx] = make_int4((int)skip, (int)k, (int)(e - k + 1), lev << 8);
-        a.visit[idx] = 0;
-        ++idx;
-      }
     }
-    if (leaf_start) {
-      int64_t e = k;
-      while (e + 1 < a.n && a.kseg[e + 1] == s && (int)a.lcp[e] >= kMaxDepth) ++e;
-      a.geom[idx] = make_float4(cx, cy, cz, h);
-      a.info[idx] = make_int4((int)(idx + 1), (int)k, (int)(e - k + 1), (ld << 8) | 1);
-      a.visit[idx] = 0;
-      // reference max_depth_: depth of the inserting body's last loop level
-      const int md = (ld == kMaxDepth && e > k) ? kMaxDepth : ld - 1;
-      atomicMax(&a.seg_depth[s], md);
-    }
+    const int64_t e = range_end(a.kseg, a.hi, a.lo, a.n, k, d);
+    const uint32_t skip = (e + 1 < a.n) ? a.nstart[e + 1] : total;
+    a.nodes[q].geom = make_float4(cx, cy, cz, h);
+    a.nodes[q].info = make_int4((int)skip, (int)k, (int)(e - k + 1), d << 8);
+    a.visit[q] = 0;
   }
 }
 
 // Parent links and child counts (children of P: P+1, skip(P+1), ... < skip(P)).
-__global__ void link_kernel(const int4* __restrict__ info, const uint32_t* __restrict__ nstart,
+__global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __restrict__ nstart,
                             int64_t n, int64_t cap, int32_t* __restrict__ parent,
                             int32_t* __restrict__ nchild) {
   const uint32_t total = nstart[n];
   if ((int64_t)total > cap) return;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
        p += (int64_t)gridDim.x * blockDim.x) {
-    const int4 ip = info[p];
+    const int4 ip = nodes[p].info;
     if (ip.w & 1) {
       nchild[p] = 0;
       continue;
@@ -535,7 +579,7 @@ __global__ void link_kernel(const int4* __restrict__ info, const uint32_t* __res
     while (c < ip.x) {
       parent[c] = (int)p;
       ++nc;
-      c = info[c].x;
+      c = nodes[c].info.x;
     }
     nchild[p] = nc;
   }
@@ -544,15 +588,15 @@ __global__ void link_kernel(const int4* __restrict__ info, const uint32_t* __res
 // Leaves: mass/com as the reference's allocateLeaf + mergeParticleIntoLeaf
 // (force_barnes_hut.cu:355-389); then the last-arriving child of each node
 // computes that node from all its children in octant order (:514-538).
-__global__ void com_kernel(const int4* __restrict__ info, const float4* __restrict__ spm,
+__global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ spm,
                            const uint32_t* __restrict__ nstart, int64_t n, int64_t cap,
                            const int32_t* __restrict__ parent, const int32_t* __restrict__ nchild,
-                           int32_t* __restrict__ visit, float4* __restrict__ com) {
+                           int32_t* __restrict__ visit) {
   const uint32_t total = nstart[n];
   if ((int64_t)total > cap) return;
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
        p += (int64_t)gridDim.x * blockDim.x) {
-    const int4 ip = info[p];
+    const int4 ip = nodes[p].info;
     if (!(ip.w & 1)) continue;
     float4 b0 = spm[ip.y];
     float m = b0.w, cx = b0.x, cy = b0.y, cz = b0.z;
@@ -564,23 +608,23 @@ __global__ void com_kernel(const int4* __restrict__ info, const float4* __restri
       cz = __fdiv_rn(__fadd_rn(__fmul_rn(cz, m), __fmul_rn(q.z, q.w)), t);
       m = t;
     }
-    com[p] = make_float4(cx, cy, cz, m);
+    nodes[p].com = make_float4(cx, cy, cz, m);
     int node = parent[p];
     while (node >= 0) {
       __threadfence();
       const int arrived = atomicAdd(&visit[node], 1);
       if (arrived != nchild[node] - 1) break;
       __threadfence();
-      const int4 in = info[node];
+      const int4 in = nodes[node].info;
       float tm = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
       int c = node + 1;
       while (c < in.x) {
-        const float4 q = __ldcg(&com[c]);
+        const float4 q = __ldcg(&nodes[c].com);
         tm = __fadd_rn(tm, q.w);
         sx = __fadd_rn(sx, __fmul_rn(q.x, q.w));
         sy = __fadd_rn(sy, __fmul_rn(q.y, q.w));
         sz = __fadd_rn(sz, __fmul_rn(q.z, q.w));
-        c = info[c].x;
+        c = nodes[c].info.x;
       }
       float4 r = make_float4(0.f, 0.f, 0.f, tm);
       if (tm > 0.0f) {
@@ -588,7 +632,7 @@ __global__ void com_kernel(const int4* __restrict__ info, const float4* __restri
         r.y = __fdiv_rn(sy, tm);
         r.z = __fdiv_rn(sz, tm);
       }
-      __stcg(&com[node], r);
+      __stcg(&nodes[node].com, r);
       node = parent[node];
     }
   }
@@ -596,9 +640,7 @@ __global__ void com_kernel(const int4* __restrict__ info, const float4* __restri
 
 // ----------------------------------------------------------------- walk --
 struct WalkArgs {
-  const float4* com;
-  const float4* geom;
-  const int4* info;
+  const Node* nodes;
   const float4* spm;
   const uint32_t* body;
   const uint32_t* nstart;
@@ -610,6 +652,8 @@ struct WalkArgs {
   int64_t n;
   int64_t cap;
   float theta2;
+  float th_lo;  // theta2 * (1 - 2^-16)
+  float th_hi;  // theta2 * (1 + 2^-16)
   float eps2;
   float G;
   int leaf_cap;
@@ -618,19 +662,20 @@ struct WalkArgs {
   float* az;
   int32_t* counts;                  // per-body interaction counts (or null)
   unsigned long long* inter_total;  // sum of interactions (or null)
+  uint32_t* task_ctr;               // zeroed before the launch
 };
 
 // The reference's opening test `size2 / dist2 < theta2` with the correctly
-// rounded quotient (force_barnes_hut.cu:222-224), decided from the MUFU
-// reciprocal whenever the approximate quotient is far (2^-16 relative) from
-// the threshold, which is almost always; only the near-threshold cases pay
-// for the IEEE division.  The outcome equals the IEEE comparison.
-__device__ __forceinline__ bool opening_accept(float size2, float d2, float theta2) {
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d2));
-  const float q = size2 * r;
-  if (q < theta2 * (1.0f - 1.52587890625e-05f)) return true;
-  if (q > theta2 * (1.0f + 1.52587890625e-05f)) return false;
+// rounded quotient (force_barnes_hut.cu:222-224), decided by two FP32
+// products against thresholds theta2 (1 -+ 2^-16) whenever size2 is not
+// within 2^-16 (relative) of theta2 * dist2 -- almost always -- and by the
+// IEEE division otherwise.  With |rounding| <= 2^-24 per product, a product
+// test that fires implies the exact quotient is below theta2 (1 - 2^-17),
+// resp. above theta2 (1 + 2^-17), so the outcome equals the IEEE comparison.
+__device__ __forceinline__ bool opening_accept(float size2, float d2, float th_lo, float th_hi,
+                                               float theta2) {
+  if (size2 < d2 * th_lo) return true;
+  if (size2 > d2 * th_hi) return false;
   return __fdiv_rn(size2, d2) < theta2;
 }
 
@@ -650,9 +695,13 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
   const uint32_t total = a.nstart[a.n];
   const bool tree_ok = (int64_t)total <= a.cap;
   const int lane = threadIdx.x & 31;
-  const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < a.ntasks;
-       t += warps) {
+  // persistent warps take the next task (32 path-consecutive targets) from a
+  // counter: the walk cost per task varies a lot, so this balances the SMs
+  while (true) {
+    uint32_t t32 = 0;
+    if (lane == 0) t32 = atomicAdd(a.task_ctr, 1u);
+    const int64_t t = __shfl_sync(0xffffffffu, t32, 0);
+    if (t >= a.ntasks) break;
     const WarpTask task = a.tasks[t];
     const int64_t k = task.first + lane;
     const bool valid = k < task.end;
@@ -663,13 +712,13 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
     int node = tree_ok ? a.seg_root[task.seg] : 0;
     const int node_end = tree_ok ? a.seg_end[task.seg] : 0;
     while (node < node_end) {
-      const float4 cm = a.com[node];
-      const int4 in = a.info[node];
+      const float4 cm = a.nodes[node].com;
+      const int4 in = a.nodes[node].info;
       if (cm.w == 0.0f) {  // force_barnes_hut.cu:172-173
         node = in.x;
         continue;
       }
-      const float4 g = a.geom[node];
+      const float4 g = a.nodes[node].geom;
       const bool active = node >= resume;
       const bool contains = fabsf(__fsub_rn(pi.x, g.x)) <= g.w &&
                             fabsf(__fsub_rn(pi.y, g.y)) <= g.w &&
@@ -699,7 +748,7 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
                   dz = __fsub_rn(cm.z, pi.z);
       const float d2 = __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), a.eps2);
       const float size2 = __fmul_rn(__fmul_rn(4.0f, g.w), g.w);
-      const bool accept = !contains && opening_accept(size2, d2, a.theta2);
+      const bool accept = !contains && opening_accept(size2, d2, a.th_lo, a.th_hi, a.theta2);
       const bool open = active && !accept;
       if (active && accept) {
         const float r = rsqrt_approx(d2);
@@ -755,9 +804,9 @@ size_t bh_state_bytes(const BHState* p) {
          h.midx_alt.bytes() + h.klo.bytes() + h.khi.bytes() + h.khi_alt.bytes() +
          h.pidx.bytes() + h.pidx_alt.bytes() + h.sk.bytes() + h.sk_alt.bytes() + h.kseg.bytes() +
          h.hist.bytes() + h.scan_ws.bytes() + h.lcp.bytes() + h.ncnt.bytes() + h.nstart.bytes() +
-         h.scalars.bytes() + h.node_com.bytes() + h.node_geom.bytes() + h.node_info.bytes() +
+         h.scalars.bytes() + h.nodes.bytes() +
          h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() + h.spm.bytes() +
-         h.inter_total.bytes();
+         h.inter_total.bytes() + h.walk_ctr.bytes();
 }
 
 size_t bh_bytes_estimate(int64_t n) { return (size_t)n * 480 + (64u << 10); }
@@ -878,29 +927,38 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err) {
   NBGB_CUDA(cudaMemsetAsync(sdepth, 0, (size_t)nseg * sizeof(int32_t), st));
   const int64_t min_cap = 2 * n + 64 * (int64_t)nseg;
   if (h.cap < min_cap) h.cap = 3 * n + 64 * (int64_t)nseg;
-  float4* geom = grow(h.node_geom, (size_t)h.cap);
-  float4* com = grow(h.node_com, (size_t)h.cap);
-  int4* info = grow(h.node_info, (size_t)h.cap);
+  Node* nodes = grow(h.nodes, (size_t)h.cap);
   int32_t* par = grow(h.node_parent, (size_t)h.cap);
   int32_t* nch = grow(h.node_nchild, (size_t)h.cap);
   int32_t* vis = grow(h.node_visit, (size_t)h.cap);
-  EmitArgs ea{kseg, lcp, hi, lo, nst, spm, h.box.ptr, h.seg_base_p, n, h.cap, geom, info, par,
+  EmitArgs ea{kseg, lcp, hi, lo, nst, spm, h.box.ptr, h.seg_base_p, n, h.cap, nodes, par,
               vis, grow(h.seg_root, (size_t)nseg), grow(h.seg_end, (size_t)nseg), sdepth, err};
   emit_nodes_kernel<<<grid1d(n), 256, 0, st>>>(ea);
   NBGB_LAUNCH_CHECK();
-  link_kernel<<<grid1d(h.cap), 256, 0, st>>>(info, nst, n, h.cap, par, nch);
+  internal_nodes_kernel<<<grid1d(h.cap), 256, 0, st>>>(ea);
   NBGB_LAUNCH_CHECK();
-  com_kernel<<<grid1d(h.cap), 256, 0, st>>>(info, spm, nst, n, h.cap, par, nch, vis, com);
+  link_kernel<<<grid1d(h.cap), 256, 0, st>>>(nodes, nst, n, h.cap, par, nch);
   NBGB_LAUNCH_CHECK();
+  com_kernel<<<grid1d(h.cap), 256, 0, st>>>(nodes, spm, nst, n, h.cap, par, nch, vis);
+  NBGB_LAUNCH_CHECK();
+}
+
+// Resident 256-thread blocks per SM of one walk instantiation.
+template <bool COUNT, bool BUCKET>
+static int walk_occupancy() {
+  static const int occ = [] {
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bh_walk_kernel<COUNT, BUCKET>, 256, 0);
+    return std::max(b, 1);
+  }();
+  return occ;
 }
 
 // Forces for every segment: acc written at each segment's arena offset.
 void bh_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, float* az, int32_t* counts,
              unsigned long long* inter_total, cudaStream_t st) {
   WalkArgs w;
-  w.com = h.node_com.ptr;
-  w.geom = h.node_geom.ptr;
-  w.info = h.node_info.ptr;
+  w.nodes = h.nodes.ptr;
   w.spm = h.spm.ptr;
   w.body = h.body;
   w.nstart = h.nstart.ptr;
@@ -912,6 +970,8 @@ void bh_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, float* az,
   w.n = h.n;
   w.cap = h.cap;
   w.theta2 = p.theta * p.theta;
+  w.th_lo = w.theta2 * (1.0f - 1.52587890625e-05f);
+  w.th_hi = w.theta2 * (1.0f + 1.52587890625e-05f);
   w.eps2 = p.softening * p.softening;
   w.G = p.G;
   w.leaf_cap = p.leaf_capacity;
@@ -920,16 +980,25 @@ void bh_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, float* az,
   w.az = az;
   w.counts = counts;
   w.inter_total = inter_total;
+  w.task_ctr = grow(h.walk_ctr, 1);
+  NBGB_CUDA(cudaMemsetAsync(w.task_ctr, 0, sizeof(uint32_t), st));
   const bool count = counts != nullptr || inter_total != nullptr;
   const bool bucket = p.leaf_capacity > 1;
-  const unsigned blocks = (unsigned)std::max<int64_t>(
-      1, std::min<int64_t>(ceil_div(h.ntasks * 32, 256), (int64_t)num_sms() * 32));
+  // one resident wave of persistent warps
+  const int64_t need = ceil_div(h.ntasks * 32, 256);
+  auto grid = [&](int occ) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(need, (int64_t)num_sms() * occ));
+  };
   if (count) {
-    if (bucket) bh_walk_kernel<true, true><<<blocks, 256, 0, st>>>(w);
-    else bh_walk_kernel<true, false><<<blocks, 256, 0, st>>>(w);
+    if (bucket)
+      bh_walk_kernel<true, true><<<grid(walk_occupancy<true, true>()), 256, 0, st>>>(w);
+    else
+      bh_walk_kernel<true, false><<<grid(walk_occupancy<true, false>()), 256, 0, st>>>(w);
   } else {
-    if (bucket) bh_walk_kernel<false, true><<<blocks, 256, 0, st>>>(w);
-    else bh_walk_kernel<false, false><<<blocks, 256, 0, st>>>(w);
+    if (bucket)
+      bh_walk_kernel<false, true><<<grid(walk_occupancy<false, true>()), 256, 0, st>>>(w);
+    else
+      bh_walk_kernel<false, false><<<grid(walk_occupancy<false, false>()), 256, 0, st>>>(w);
   }
   NBGB_LAUNCH_CHECK();
 }
@@ -972,13 +1041,12 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
 }
 
 // ------------------------------------------------------------- export --
-__global__ void export_nodes_kernel(const float4* __restrict__ com, const float4* __restrict__ geom,
-                                    const int4* __restrict__ info, const uint32_t* __restrict__ body,
+__global__ void export_nodes_kernel(const Node* __restrict__ nodes, const uint32_t* __restrict__ body,
                                     int64_t total, nbgb_octree_node* __restrict__ out) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total;
        p += (int64_t)gridDim.x * blockDim.x) {
-    const int4 in = info[p];
-    const float4 g = geom[p], cm = com[p];
+    const int4 in = nodes[p].info;
+    const float4 g = nodes[p].geom, cm = nodes[p].com;
     nbgb_octree_node& o = out[p];
     o.center[0] = g.x;
     o.center[1] = g.y;
@@ -996,14 +1064,14 @@ __global__ void export_nodes_kernel(const float4* __restrict__ com, const float4
   }
 }
 
-__global__ void export_children_kernel(const int4* __restrict__ info,
+__global__ void export_children_kernel(const Node* __restrict__ nodes,
                                        const int32_t* __restrict__ parent,
                                        const u64* __restrict__ hi, const u64* __restrict__ lo,
                                        int64_t total, nbgb_octree_node* __restrict__ out) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < total;
        p += (int64_t)gridDim.x * blockDim.x) {
     if (parent[p] < 0) continue;  // a root
-    const int4 in = info[p];
+    const int4 in = nodes[p].info;
     const int d = in.w >> 8;
     const int64_t f = in.y;
     const uint32_t oct = (d <= kHiLevels) ? (uint32_t)((hi[f] >> (3 * (kHiLevels - d))) & 7u)
@@ -1079,9 +1147,8 @@ nbgb_status nbgb_bh_copy_nodes(nbgb_calculator* c, nbgb_octree_node* nodes, size
   if (cudaMalloc(&d, (size_t)std::max<int64_t>(total, 1) * sizeof(nbgb_octree_node)) != cudaSuccess)
     return NBGB_ERR_OOM;
   unsigned blocks = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, 256), 4096));
-  export_nodes_kernel<<<blocks, 256, 0, c->stream>>>(h.node_com.ptr, h.node_geom.ptr,
-                                                     h.node_info.ptr, h.body, total, d);
-  export_children_kernel<<<blocks, 256, 0, c->stream>>>(h.node_info.ptr, h.node_parent.ptr,
+  export_nodes_kernel<<<blocks, 256, 0, c->stream>>>(h.nodes.ptr, h.body, total, d);
+  export_children_kernel<<<blocks, 256, 0, c->stream>>>(h.nodes.ptr, h.node_parent.ptr,
                                                         h.khi.ptr, h.klo.ptr, total, d);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
