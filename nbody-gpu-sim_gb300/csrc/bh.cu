@@ -63,8 +63,8 @@ constexpr int kMaxDepth = 32;  // force_barnes_hut.cu:24
 struct __align__(16) Node {
   float4 com;   // centre of mass, total mass
   float4 geom;  // cube centre, half size
-  int4 info;    // skip (next node outside the subtree), first body, body count,
-                // depth << 8 | leaf
+  int4 info;    // skip (next node outside the subtree), depth << 8 | leaf,
+                // first body, body count
   float4 pad;
 };
 
@@ -485,7 +485,7 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
       const int64_t send = a.base[s + 1];  // one past the segment's last position
       const uint32_t skip = (send < a.n) ? a.nstart[send] : total;
       a.nodes[idx].geom = make_float4(b.center[0], b.center[1], b.center[2], b.half);
-      a.nodes[idx].info = make_int4((int)skip, (int)k, (int)(send - k), 0);
+      a.nodes[idx].info = make_int4((int)skip, 0, (int)k, (int)(send - k));
       a.parent[idx] = -1;
       a.visit[idx] = 0;
       a.seg_root[s] = (int32_t)idx;
@@ -513,7 +513,7 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
       int64_t e = k;
       while (e + 1 < a.n && a.kseg[e + 1] == s && (int)a.lcp[e] >= kMaxDepth) ++e;
       a.nodes[idx].geom = make_float4(cx, cy, cz, h);
-      a.nodes[idx].info = make_int4((int)(idx + 1), (int)k, (int)(e - k + 1), (ld << 8) | 1);
+      a.nodes[idx].info = make_int4((int)(idx + 1), (ld << 8) | 1, (int)k, (int)(e - k + 1));
       a.parent[idx] = -1;
       a.visit[idx] = 0;
       // reference max_depth_: depth of the inserting body's last loop level
@@ -557,7 +557,7 @@ __global__ void internal_nodes_kernel(EmitArgs a) {
     const int64_t e = range_end(a.kseg, a.hi, a.lo, a.n, k, d);
     const uint32_t skip = (e + 1 < a.n) ? a.nstart[e + 1] : total;
     a.nodes[q].geom = make_float4(cx, cy, cz, h);
-    a.nodes[q].info = make_int4((int)skip, (int)k, (int)(e - k + 1), d << 8);
+    a.nodes[q].info = make_int4((int)skip, d << 8, (int)k, (int)(e - k + 1));
     a.visit[q] = 0;
   }
 }
@@ -571,7 +571,7 @@ __global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __re
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
        p += (int64_t)gridDim.x * blockDim.x) {
     const int4 ip = nodes[p].info;
-    if (ip.w & 1) {
+    if (ip.y & 1) {
       nchild[p] = 0;
       continue;
     }
@@ -597,11 +597,11 @@ __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ 
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
        p += (int64_t)gridDim.x * blockDim.x) {
     const int4 ip = nodes[p].info;
-    if (!(ip.w & 1)) continue;
-    float4 b0 = spm[ip.y];
+    if (!(ip.y & 1)) continue;
+    float4 b0 = spm[ip.z];
     float m = b0.w, cx = b0.x, cy = b0.y, cz = b0.z;
-    for (int j = 1; j < ip.z; ++j) {
-      const float4 q = spm[ip.y + j];
+    for (int j = 1; j < ip.w; ++j) {
+      const float4 q = spm[ip.z + j];
       const float t = __fadd_rn(m, q.w);
       cx = __fdiv_rn(__fadd_rn(__fmul_rn(cx, m), __fmul_rn(q.x, q.w)), t);
       cy = __fdiv_rn(__fadd_rn(__fmul_rn(cy, m), __fmul_rn(q.y, q.w)), t);
@@ -639,6 +639,13 @@ __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ 
 }
 
 // ----------------------------------------------------------------- walk --
+// Centre of mass and cube of a node in one 256-bit load (read-only path).
+__device__ __forceinline__ void ld_node(const Node* p, float4& cm, float4& g) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(cm.x), "=f"(cm.y), "=f"(cm.z), "=f"(cm.w), "=f"(g.x), "=f"(g.y), "=f"(g.z), "=f"(g.w)
+      : "l"(p));
+}
+
 struct WalkArgs {
   const Node* nodes;
   const float4* spm;
@@ -712,18 +719,19 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
     int node = tree_ok ? a.seg_root[task.seg] : 0;
     const int node_end = tree_ok ? a.seg_end[task.seg] : 0;
     while (node < node_end) {
-      const float4 cm = a.nodes[node].com;
-      const int4 in = a.nodes[node].info;
+      // one 32-byte load (centre of mass + cube), one 8-byte load (skip, flags)
+      float4 cm, g;
+      ld_node(&a.nodes[node], cm, g);
+      const int2 in = __ldg(reinterpret_cast<const int2*>(&a.nodes[node].info));
       if (cm.w == 0.0f) {  // force_barnes_hut.cu:172-173
         node = in.x;
         continue;
       }
-      const float4 g = a.nodes[node].geom;
       const bool active = node >= resume;
       const bool contains = fabsf(__fsub_rn(pi.x, g.x)) <= g.w &&
                             fabsf(__fsub_rn(pi.y, g.y)) <= g.w &&
                             fabsf(__fsub_rn(pi.z, g.z)) <= g.w;
-      if (in.w & 1) {  // leaf
+      if (in.y & 1) {  // leaf
         if (active) {
           float me = cm.w, cx = cm.x, cy = cm.y, cz = cm.z;
           bool use = true;
@@ -759,18 +767,21 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
         if (COUNT) ++cnt;
         resume = in.x;
       }
-      if (BUCKET && in.z <= a.leaf_cap) {
-        if (open) {
-          for (int j = 0; j < in.z; ++j) {
-            const int64_t s = (int64_t)in.y + j;
-            if (s == k) continue;
-            const float4 q = a.spm[s];
-            bh_add(q.x, q.y, q.z, q.w, pi.x, pi.y, pi.z, a.eps2, sx, sy, sz);
-            if (COUNT) ++cnt;
+      if (BUCKET) {
+        const int4 full = a.nodes[node].info;  // first, count
+        if (full.w <= a.leaf_cap) {
+          if (open) {
+            for (int j = 0; j < full.w; ++j) {
+              const int64_t s = (int64_t)full.z + j;
+              if (s == k) continue;
+              const float4 q = a.spm[s];
+              bh_add(q.x, q.y, q.z, q.w, pi.x, pi.y, pi.z, a.eps2, sx, sy, sz);
+              if (COUNT) ++cnt;
+            }
           }
+          node = in.x;
+          continue;
         }
-        node = in.x;
-        continue;
       }
       node = __any_sync(0xffffffffu, open) ? node + 1 : in.x;
     }
@@ -1056,10 +1067,10 @@ __global__ void export_nodes_kernel(const Node* __restrict__ nodes, const uint32
     o.center_of_mass[1] = cm.y;
     o.center_of_mass[2] = cm.z;
     o.total_mass = cm.w;
-    o.is_leaf = (uint8_t)(in.w & 1);
+    o.is_leaf = (uint8_t)(in.y & 1);
     o.pad_[0] = o.pad_[1] = o.pad_[2] = 0;
-    o.particle_count = in.z;
-    o.particle_index = (in.w & 1) ? (int32_t)body[in.y] : -1;
+    o.particle_count = in.w;
+    o.particle_index = (in.y & 1) ? (int32_t)body[in.z] : -1;
     for (int j = 0; j < 8; ++j) o.children[j] = -1;
   }
 }
@@ -1072,8 +1083,8 @@ __global__ void export_children_kernel(const Node* __restrict__ nodes,
        p += (int64_t)gridDim.x * blockDim.x) {
     if (parent[p] < 0) continue;  // a root
     const int4 in = nodes[p].info;
-    const int d = in.w >> 8;
-    const int64_t f = in.y;
+    const int d = in.y >> 8;
+    const int64_t f = in.z;
     const uint32_t oct = (d <= kHiLevels) ? (uint32_t)((hi[f] >> (3 * (kHiLevels - d))) & 7u)
                                           : (uint32_t)((lo[f] >> (3 * (kMaxDepth - d))) & 7u);
     out[parent[p]].children[oct] = (int32_t)p;
