@@ -258,6 +258,8 @@ def gpu_arm(args, rank, world, local):
     dint = s1["direct_kernel_interactions"] - s0["direct_kernel_interactions"]
     dms = s1["direct_kernel_ms"] - s0["direct_kernel_ms"]
     bh_int = s1["bh_interactions"] - s0["bh_interactions"]
+    walk_ms = s1["bh_walk_ms"] - s0["bh_walk_ms"]
+    bh_bodies = s1["bh_bodies"]
     launches = s1["kernel_launches"] - s0["kernel_launches"]
     tuned = s1["direct_config"]
     ens.close()
@@ -311,8 +313,13 @@ def gpu_arm(args, rank, world, local):
         cpu = cpu_baseline(nbgb, stream, args.cpu_seconds)
 
         ffma_peak = ffma.value
-        achieved = 20.0 * dint / (dms / 1e3) / 1e12 if dms > 0 else None
+        d_achieved = 20.0 * dint / (dms / 1e3) / 1e12 if dms > 0 else None
+        w_achieved = 20.0 * bh_int / (walk_ms / 1e3) / 1e12 if walk_ms > 0 else None
+        walk_share = (walk_ms / 1e3) / elapsed_s if elapsed_s > 0 else None
         direct_share = (dms / 1e3) / elapsed_s if elapsed_s > 0 else None
+        # DRAM bytes of one walk launch: ncu capture at N = 1,048,576 (two
+        # Plummer spheres, 147.6 MB read + written), scaled by the bodies walked
+        walk_traffic = 147.6e6 * bh_bodies / 1048576 if bh_bodies else None
         clocks = clk.summary()
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -349,15 +356,24 @@ def gpu_arm(args, rank, world, local):
                              "API: host arrays submitted, results polled to the host"}
                     if serve_rep else None),
             "roofline": {
-                "kernel": "ens_direct_kernel (direct-sum work queue)",
-                "bound": "fp32", "achieved": achieved, "peak": ffma_peak, "unit": "TFLOP/s",
-                "frac": (achieved / ffma_peak) if achieved else None,
-                "traffic": None,
+                "kernel": "bh_walk_kernel (batched Barnes-Hut walk, all resident BH systems)",
+                "bound": "fp32", "achieved": w_achieved, "peak": ffma_peak, "unit": "TFLOP/s",
+                "frac": (w_achieved / ffma_peak) if w_achieved else None,
+                "traffic": walk_traffic,
+                "traffic_source": "ncu dram__bytes_read+write of one walk at N=1,048,576 "
+                                  "(profiles/bh_walk_two_plummer_1M.md), scaled by bodies walked",
+                "algorithmic_bytes": 64 * 1.5 * bh_bodies + 28 * bh_bodies if bh_bodies else None,
                 "peak_source": "measured in-process: FFMA chains on every SM "
                                "(nbgb_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
-                "flops_per_interaction": 20, "share_of_tick": direct_share,
+                "flops_per_interaction": 20, "share_of_tick": walk_share,
+                "walk_ms_per_tick": walk_ms / args.steps,
+                "note": "issue-bound tree walk: ~78 thread instructions per accepted "
+                        "interaction, 83 % issue-active (ncu)",
                 "hbm_peak_gbs_measured": measured_peaks().get("hbm_gbs"),
             },
+            "direct_kernel": {"kernel": "ens_direct_kernel (direct-sum work queue)",
+                              "achieved_tflops": d_achieved, "share_of_tick": direct_share,
+                              "note": "overlaps the Barnes-Hut chain on another stream"},
             "fp32_peaks": {"ffma_tflops": ffma.value, "ffma2_tflops": ffma2.value,
                            "mufu_gops": mufu.value},
             "cpu_baseline": cpu,

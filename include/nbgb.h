@@ -300,6 +300,8 @@ typedef struct nbgb_ensemble_stats {
   double direct_kernel_ms;      /* summed device time of the direct work-queue kernel */
   double direct_kernel_interactions; /* interactions those launches computed */
   int64_t kernel_launches;      /* kernels launched by ticks (graph kernel nodes counted) */
+  double bh_walk_ms;            /* summed device time of the batched Barnes-Hut walk */
+  int64_t bh_bodies;            /* bodies in the current Barnes-Hut segments */
 } nbgb_ensemble_stats;
 
 void nbgb_ensemble_config_default(nbgb_ensemble_config* cfg);

@@ -298,10 +298,15 @@ struct nbgb_ensemble {
   bool bh_dirty = true;   // Barnes-Hut resident set changed
   int64_t bh_n = 0;       // bodies in the Barnes-Hut segments
   int bh_stable = 0;      // ticks since the set last changed
-  cudaGraph_t bh_graph = nullptr;
+  cudaGraph_t bh_graph = nullptr;  // the tree build
   cudaGraphExec_t bh_exec = nullptr;
   int64_t bh_graph_kernels = 0;
   cudaEvent_t ev_bh = nullptr;
+  // walk timing ring (events around each tick's walk on bh_stream)
+  cudaEvent_t wev0[kTimingRing] = {}, wev1[kTimingRing] = {};
+  bool wev_used[kTimingRing] = {};
+  int wev_next = 0;
+  double walk_ms = 0.0;
   // arena
   int64_t cap = 0;  // bodies
   DevBuf<double> x, y, z, vx, vy, vz;
@@ -461,41 +466,54 @@ static void bh_tables(nbgb_ensemble* e) {
   bh_reserve_async(*e->bh);
 }
 
-// Build + walk of every resident Barnes-Hut system, enqueued on bh_stream.
-static void bh_pass(nbgb_ensemble* e) {
-  const BHWalkParams wp{e->cfg.G, e->cfg.softening, e->cfg.theta, e->cfg.leaf_capacity};
-  bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr);
-  bh_walk(*e->bh, wp, e->ax.ptr, e->ay.ptr, e->az.ptr, nullptr, e->d_bh_inter.ptr, e->bh_stream);
+static void harvest_walk(nbgb_ensemble* e, int k) {
+  if (!e->wev_used[k]) return;
+  NBGB_CUDA(cudaEventSynchronize(e->wev1[k]));
+  float ms = 0.f;
+  NBGB_CUDA(cudaEventElapsedTime(&ms, e->wev0[k], e->wev1[k]));
+  e->wev_used[k] = false;
+  e->walk_ms += ms;
 }
 
-// Launches the pass: eagerly right after the set changed, then (with graphs
-// enabled) as a graph captured on the first stable tick, when every buffer
-// of the pass has been allocated.  Returns the kernels the graph launched.
+// Tree build of every resident Barnes-Hut system, enqueued on bh_stream:
+// eagerly right after the set changed, then (with graphs enabled) as a
+// graph captured on the first stable tick, when every buffer of the build
+// has been allocated.  Then the walk, between timing events.  Returns the
+// kernels a graph launched.
 static int64_t run_bh_pass(nbgb_ensemble* e) {
+  int64_t graph_kernels = 0;
   if (e->bh_exec) {
     NBGB_CUDA(cudaGraphLaunch(e->bh_exec, e->bh_stream));
-    return e->bh_graph_kernels;
+    graph_kernels = e->bh_graph_kernels;
+  } else if (!e->cfg.use_graphs || e->bh_stable < 1) {
+    bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr);
+  } else {
+    const int64_t l0 = t_launches;
+    NBGB_CUDA(cudaStreamBeginCapture(e->bh_stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr);
+    } catch (...) {
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(e->bh_stream, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    NBGB_CUDA(cudaStreamEndCapture(e->bh_stream, &e->bh_graph));
+    NBGB_CUDA(cudaGraphInstantiate(&e->bh_exec, e->bh_graph, 0));
+    e->bh_graph_kernels = t_launches - l0;
+    t_launches = l0;  // captured, not launched: the graph launch counts them
+    NBGB_CUDA(cudaGraphLaunch(e->bh_exec, e->bh_stream));
+    graph_kernels = e->bh_graph_kernels;
   }
-  if (!e->cfg.use_graphs || e->bh_stable < 1) {
-    bh_pass(e);
-    return 0;
-  }
-  const int64_t l0 = t_launches;
-  NBGB_CUDA(cudaStreamBeginCapture(e->bh_stream, cudaStreamCaptureModeThreadLocal));
-  try {
-    bh_pass(e);
-  } catch (...) {
-    cudaGraph_t g = nullptr;
-    cudaStreamEndCapture(e->bh_stream, &g);
-    if (g) cudaGraphDestroy(g);
-    throw;
-  }
-  NBGB_CUDA(cudaStreamEndCapture(e->bh_stream, &e->bh_graph));
-  NBGB_CUDA(cudaGraphInstantiate(&e->bh_exec, e->bh_graph, 0));
-  e->bh_graph_kernels = t_launches - l0;
-  t_launches = l0;  // captured, not launched: the graph launch below counts them
-  NBGB_CUDA(cudaGraphLaunch(e->bh_exec, e->bh_stream));
-  return e->bh_graph_kernels;
+  const int k = e->wev_next % kTimingRing;
+  harvest_walk(e, k);
+  NBGB_CUDA(cudaEventRecord(e->wev0[k], e->bh_stream));
+  const BHWalkParams wp{e->cfg.G, e->cfg.softening, e->cfg.theta, e->cfg.leaf_capacity};
+  bh_walk(*e->bh, wp, e->ax.ptr, e->ay.ptr, e->az.ptr, nullptr, e->d_bh_inter.ptr, e->bh_stream);
+  NBGB_CUDA(cudaEventRecord(e->wev1[k], e->bh_stream));
+  e->wev_used[k] = true;
+  e->wev_next++;
+  return graph_kernels;
 }
 
 // Admits, in FIFO order, every queued request that fits the resident cap,
@@ -634,7 +652,10 @@ static void harvest(nbgb_ensemble* e, int k) {
 }
 
 static void harvest_all(nbgb_ensemble* e) {
-  for (int k = 0; k < kTimingRing; ++k) harvest(e, k);
+  for (int k = 0; k < kTimingRing; ++k) {
+    harvest(e, k);
+    harvest_walk(e, k);
+  }
 }
 
 // Tuning schedule: every configuration runs two ticks; once all are
@@ -832,6 +853,8 @@ nbgb_status nbgb_ensemble_create(const nbgb_ensemble_config* cfg, nbgb_ensemble*
     for (int k = 0; k < kTimingRing; ++k) {
       NBGB_CUDA(cudaEventCreate(&e->tev0[k]));
       NBGB_CUDA(cudaEventCreate(&e->tev1[k]));
+      NBGB_CUDA(cudaEventCreate(&e->wev0[k]));
+      NBGB_CUDA(cudaEventCreate(&e->wev1[k]));
     }
     NBGB_CUDA(cudaEventCreateWithFlags(&e->ev_kd, cudaEventDisableTiming));
     NBGB_CUDA(cudaEventCreateWithFlags(&e->ev_bh, cudaEventDisableTiming));
@@ -858,6 +881,8 @@ nbgb_status nbgb_ensemble_destroy(nbgb_ensemble* e) {
     for (int k = 0; k < kTimingRing; ++k) {
       cudaEventDestroy(e->tev0[k]);
       cudaEventDestroy(e->tev1[k]);
+      cudaEventDestroy(e->wev0[k]);
+      cudaEventDestroy(e->wev1[k]);
     }
     cudaEventDestroy(e->ev_kd);
     if (e->stage_evt) cudaEventDestroy(e->stage_evt);
@@ -967,6 +992,8 @@ nbgb_status nbgb_ensemble_get_stats(nbgb_ensemble* e, nbgb_ensemble_stats* s) {
   }
   *s = e->st;
   s->bh_interactions = (double)bh_inter;
+  s->bh_walk_ms = e->walk_ms;
+  s->bh_bodies = e->bh_n;
   s->direct_kernel_ms = e->dk_ms;
   s->direct_kernel_interactions = e->dk_inter;
   s->resident = (int32_t)e->resident.size();

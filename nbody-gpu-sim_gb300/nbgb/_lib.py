@@ -53,7 +53,8 @@ class EnsembleStats(C.Structure):
                 ("queued", C.c_int32), ("bytes_reserved", C.c_uint64),
                 ("direct_config", C.c_int32), ("tuning", C.c_int32),
                 ("direct_kernel_ms", C.c_double), ("direct_kernel_interactions", C.c_double),
-                ("kernel_launches", C.c_int64)]
+                ("kernel_launches", C.c_int64), ("bh_walk_ms", C.c_double),
+                ("bh_bodies", C.c_int64)]
 
 
 assert C.sizeof(OctreeNode) == 76

@@ -176,6 +176,7 @@ def test_batched_bh_bitwise_vs_calculator(nb):
     ens.close()
     assert len(got) == len(reqs)
     assert st["bh_interactions"] > 0 and st["direct_interactions"] == 0
+    assert st["bh_walk_ms"] > 0
     for rid, s in got.items():
         pos = {k: s[k].astype(np.float32) for k in ("x", "y", "z")}
         ref = _calc_bh(nb, pos, s["m"])
