@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=192)
     ap.add_argument("--serve-max-s", type=float, default=90.0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-budget-s", type=float, default=120.0,
+                    help="--impl reference: CPU seconds spread over warmup + steps")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--case", choices=["direct", "bh", "bh8", "hash", "precision"], default=None,
@@ -217,7 +219,7 @@ def gpu_arm(args, rank, world, local):
     ffma, ffma2, mufu = C.c_double(), C.c_double(), C.c_double()
     nbgb.check(lib.nbgb_measure_fp32_peak(C.byref(ffma), C.byref(ffma2), C.byref(mufu)))
 
-    stream_seed = 5 + 1000 * rank
+    stream_seed = shard_seed(rank)
     stream = nbgb.ics.ensemble_requests(4096, seed=stream_seed)
     S = args.resident
     # --- batched, saturation --------------------------------------------------
@@ -266,16 +268,7 @@ def gpu_arm(args, rank, world, local):
     del states
 
     # --- reduction over ranks ---------------------------------------------------
-    t_max = elapsed_s
-    ps_tot = ps
-    if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([elapsed_s], dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
-        pt = torch.tensor([float(ps)], dtype=torch.float64)
-        dist.all_reduce(pt, op=dist.ReduceOp.SUM)
-        ps_tot = float(pt.item())
+    t_max, ps_tot = reduce_over_ranks(elapsed_s, ps, world)
     value = ps_tot / t_max
 
     out = {}
@@ -408,10 +401,33 @@ def plain_arm(nbgb, reqs, steps) -> dict:
             "ms_per_step_by_n": [[n, 1e3 * t] for n, t in per[:12]]}
 
 
+def cpu_step(orc, nbgb, r) -> tuple[float, float]:
+    """One Velocity-Verlet step of request r on the host through the
+    reference's CPU path as restated in oracle/ (pair-function direct sum in
+    reference order for N <= 8192; the reference insertion octree + walk for
+    the Barnes-Hut systems).  Returns (particle-steps, seconds)."""
+    s = make_state(nbgb, r)
+    x, y, z, m = s["x"].copy(), s["y"].copy(), s["z"].copy(), s["m"]
+    vx, vy, vz = s["vx"].copy(), s["vy"].copy(), s["vz"].copy()
+    if r["n"] <= 8192:
+        ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)  # a(t) of a running system
+        t0 = time.perf_counter()
+        ox, oy, oz = ax.copy(), ay.copy(), az.copy()
+        orc.update_positions(x, y, z, vx, vy, vz, ax, ay, az, DT)
+        ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
+        orc.update_velocities(vx, vy, vz, ox, oy, oz, ax, ay, az, DT)
+        return float(r["n"]), time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bmin, bmax = orc.bbox(x, y, z)
+    _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
+    nodes, _, _ = orc.build_octree(x, y, z, m, si, bmin, bmax)
+    orc.bh_forces(nodes, x, y, z, m, 0.5, 1.0, EPS)
+    return float(r["n"]), time.perf_counter() - t0
+
+
 def cpu_baseline(nbgb, stream, seconds) -> dict:
-    """The reference's CPU path (pair-function direct sum in reference order,
-    Velocity-Verlet formulae; the reference insertion octree + walk for the
-    Barnes-Hut systems) restated in oracle/, one step per sampled system."""
+    """The reference's CPU path on a bounded sample of the request stream,
+    one step per sampled system (cpu_step)."""
     from oracle.oracle import Oracle
     orc = Oracle()
     ps, t = 0.0, 0.0
@@ -419,27 +435,8 @@ def cpu_baseline(nbgb, stream, seconds) -> dict:
     for r in stream:
         if t > seconds:
             break
-        s = make_state(nbgb, r)
-        x, y, z, m = s["x"].copy(), s["y"].copy(), s["z"].copy(), s["m"]
-        vx, vy, vz = s["vx"].copy(), s["vy"].copy(), s["vz"].copy()
-        if r["n"] <= 8192:
-            ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)  # a(t) of a running system
-            t0 = time.perf_counter()
-            ox, oy, oz = ax.copy(), ay.copy(), az.copy()
-            orc.update_positions(x, y, z, vx, vy, vz, ax, ay, az, DT)
-            ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
-            orc.update_velocities(vx, vy, vz, ox, oy, oz, ax, ay, az, DT)
-            steps = 1
-            dt = time.perf_counter() - t0
-        else:
-            t0 = time.perf_counter()
-            bmin, bmax = orc.bbox(x, y, z)
-            _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
-            nodes, _, _ = orc.build_octree(x, y, z, m, si, bmin, bmax)
-            orc.bh_forces(nodes, x, y, z, m, 0.5, 1.0, EPS)
-            steps = 1
-            dt = time.perf_counter() - t0
-        ps += r["n"] * steps
+        p, dt = cpu_step(orc, nbgb, r)
+        ps += p
         t += dt
         count += 1
     return {"value": ps / t if t > 0 else None, "unit": UNIT, "cores": orc.num_threads(),
@@ -449,43 +446,55 @@ def cpu_baseline(nbgb, stream, seconds) -> dict:
                       f"reference insertion octree + walk), {t:.1f} s of CPU time"}
 
 
+# ------------------------------------------------------------ multi-rank --
+def shard_seed(rank: int) -> int:
+    """Seed of rank's own shard of the request stream (weak scaling: every
+    rank serves an independent stream of the same distribution)."""
+    return 5 + 1000 * rank
+
+
+def reduce_over_ranks(elapsed_s: float, particle_steps: float, world: int) -> tuple[float, float]:
+    """(max elapsed over ranks, particle-steps summed over ranks); the only
+    collectives of the benchmark (no data-path exchange)."""
+    if world <= 1:
+        return elapsed_s, float(particle_steps)
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([elapsed_s], dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    pt = torch.tensor([float(particle_steps)], dtype=torch.float64)
+    dist.all_reduce(pt, op=dist.ReduceOp.SUM)
+    return float(tt.item()), float(pt.item())
+
+
 # ----------------------------------------------------------- reference arm --
 def reference_arm(args, rank, world):
+    """The reference's CPU path (cpu_step) on the host cores, rank 0 only:
+    each step a bounded sample of the same request stream."""
     if rank != 0:
         return None
     import nbgb  # only for the request stream and the initial conditions
-    stream = nbgb.ics.ensemble_requests(4096, seed=5)
+    stream = nbgb.ics.ensemble_requests(4096, seed=shard_seed(0))
     from oracle.oracle import Oracle
     orc = Oracle()
-    per_step = max(2.0, 120.0 / max(args.steps + args.warmup, 1))
+    per_step = min(20.0, max(0.5, args.ref_budget_s / max(args.steps + args.warmup, 1)))
     results = []
     idx = 0
     for k in range(args.warmup + args.steps):
         ps, t = 0.0, 0.0
         while t < per_step and idx < len(stream):
-            r = stream[idx]
+            p, dt = cpu_step(orc, nbgb, stream[idx])
             idx += 1
-            if r["n"] > 8192:
-                continue  # a bounded sample of the direct part keeps each step short
-            s = make_state(nbgb, r)
-            x, y, z, m = s["x"].copy(), s["y"].copy(), s["z"].copy(), s["m"]
-            vx, vy, vz = s["vx"].copy(), s["vy"].copy(), s["vz"].copy()
-            ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
-            t0 = time.perf_counter()
-            ox, oy, oz = ax.copy(), ay.copy(), az.copy()
-            orc.update_positions(x, y, z, vx, vy, vz, ax, ay, az, DT)
-            ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
-            orc.update_velocities(vx, vy, vz, ox, oy, oz, ax, ay, az, DT)
-            t += time.perf_counter() - t0
-            ps += r["n"]
+            ps += p
+            t += dt
         if k >= args.warmup:
             results.append((ps, t))
     tot_ps = sum(p for p, _ in results)
     tot_t = sum(t for _, t in results)
     value = tot_ps / tot_t if tot_t > 0 else 0.0
-    sample = (f"per step: direct-method systems (N<=8192) of the request stream, one "
-              f"Velocity-Verlet step each, ~{per_step:.0f} s of CPU work; reference pair "
-              f"function in reference order")
+    sample = (f"per step: consecutive systems of the request stream, one Velocity-Verlet "
+              f"step each, ~{per_step:.1f} s of CPU work (direct: reference pair function "
+              f"order; N>8192: reference insertion octree + walk)")
     return {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup,
