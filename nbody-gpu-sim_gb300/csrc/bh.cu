@@ -65,8 +65,23 @@ struct __align__(16) Node {
   float4 geom;  // cube centre, half size
   int4 info;    // skip (next node outside the subtree), depth << 8 | leaf,
                 // first body, body count
-  float4 pad;
+  int2 walk;    // for the walk: skip | leaf << 31 | zero mass << 30, bits of 4 h^2
+  int2 pad;
 };
+
+constexpr uint32_t kWalkLeaf = 1u << 31;
+constexpr uint32_t kWalkZero = 1u << 30;
+constexpr int64_t kMaxWalkNodes = (int64_t)1 << 30;  // skip indices below the flag bits
+
+// The walk record of a node whose centre of mass is final: skip and flags,
+// and the opening test's size2 = 4 h^2 (force_barnes_hut.cu:222) rounded as
+// the reference rounds it.
+__device__ __forceinline__ int2 walk_record(const int4& in, float h, float mass) {
+  uint32_t w = (uint32_t)in.x;
+  if (in.y & 1) w |= kWalkLeaf;
+  if (mass == 0.0f) w |= kWalkZero;
+  return make_int2((int)w, __float_as_int(__fmul_rn(__fmul_rn(4.0f, h), h)));
+}
 
 struct BHState {
   // segment tables (device; single-system calls fill one segment)
@@ -609,6 +624,7 @@ __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ 
       m = t;
     }
     nodes[p].com = make_float4(cx, cy, cz, m);
+    nodes[p].walk = walk_record(ip, nodes[p].geom.w, m);
     int node = parent[p];
     while (node >= 0) {
       __threadfence();
@@ -633,6 +649,7 @@ __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ 
         r.z = __fdiv_rn(sz, tm);
       }
       __stcg(&nodes[node].com, r);
+      nodes[node].walk = walk_record(in, nodes[node].geom.w, r.w);
       node = parent[node];
     }
   }
@@ -719,23 +736,23 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
     int node = tree_ok ? a.seg_root[task.seg] : 0;
     const int node_end = tree_ok ? a.seg_end[task.seg] : 0;
     while (node < node_end) {
-      // one 32-byte load (centre of mass + cube), one 8-byte load (skip, flags)
+      // one 32-byte load (centre of mass + cube), one 8-byte load (skip and
+      // flags, size2)
       float4 cm, g;
       ld_node(&a.nodes[node], cm, g);
-      const int2 in = __ldg(reinterpret_cast<const int2*>(&a.nodes[node].info));
-      if (cm.w == 0.0f) {  // force_barnes_hut.cu:172-173
-        node = in.x;
-        continue;
-      }
-      const bool active = node >= resume;
-      const bool contains = fabsf(__fsub_rn(pi.x, g.x)) <= g.w &&
-                            fabsf(__fsub_rn(pi.y, g.y)) <= g.w &&
-                            fabsf(__fsub_rn(pi.z, g.z)) <= g.w;
-      if (in.y & 1) {  // leaf
-        if (active) {
+      const int2 wr = __ldg(&a.nodes[node].walk);
+      const int skip = wr.x & (int)(kWalkZero - 1u);
+      if ((uint32_t)wr.x >= kWalkZero) {  // a leaf, or zero mass
+        if ((uint32_t)wr.x & kWalkZero) {  // force_barnes_hut.cu:172-173
+          node = skip;
+          continue;
+        }
+        // leaf (force_barnes_hut.cu:185-203)
+        if (node >= resume) {
           float me = cm.w, cx = cm.x, cy = cm.y, cz = cm.z;
           bool use = true;
-          if (contains) {
+          if (fabsf(__fsub_rn(pi.x, g.x)) <= g.w && fabsf(__fsub_rn(pi.y, g.y)) <= g.w &&
+              fabsf(__fsub_rn(pi.z, g.z)) <= g.w) {
             me = __fsub_rn(cm.w, pi.w);
             use = me > 0.0f;
             if (use) {
@@ -749,13 +766,18 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
             if (COUNT) ++cnt;
           }
         }
-        node = in.x;
+        node = skip;
         continue;
       }
+      // internal node (force_barnes_hut.cu:205-243)
+      const bool active = node >= resume;
+      const bool contains = fabsf(__fsub_rn(pi.x, g.x)) <= g.w &&
+                            fabsf(__fsub_rn(pi.y, g.y)) <= g.w &&
+                            fabsf(__fsub_rn(pi.z, g.z)) <= g.w;
       const float dx = __fsub_rn(cm.x, pi.x), dy = __fsub_rn(cm.y, pi.y),
                   dz = __fsub_rn(cm.z, pi.z);
       const float d2 = __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), a.eps2);
-      const float size2 = __fmul_rn(__fmul_rn(4.0f, g.w), g.w);
+      const float size2 = __int_as_float(wr.y);
       const bool accept = !contains && opening_accept(size2, d2, a.th_lo, a.th_hi, a.theta2);
       const bool open = active && !accept;
       if (active && accept) {
@@ -765,7 +787,7 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
         sy = fmaf(f, dy, sy);
         sz = fmaf(f, dz, sz);
         if (COUNT) ++cnt;
-        resume = in.x;
+        resume = skip;
       }
       if (BUCKET) {
         const int4 full = a.nodes[node].info;  // first, count
@@ -779,11 +801,11 @@ __global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
               if (COUNT) ++cnt;
             }
           }
-          node = in.x;
+          node = skip;
           continue;
         }
       }
-      node = __any_sync(0xffffffffu, open) ? node + 1 : in.x;
+      node = __any_sync(0xffffffffu, open) ? node + 1 : skip;
     }
     if (valid) {
       const int64_t i = a.sv.arena(a.body[k]);
@@ -938,6 +960,8 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err) {
   NBGB_CUDA(cudaMemsetAsync(sdepth, 0, (size_t)nseg * sizeof(int32_t), st));
   const int64_t min_cap = 2 * n + 64 * (int64_t)nseg;
   if (h.cap < min_cap) h.cap = 3 * n + 64 * (int64_t)nseg;
+  if (h.cap >= kMaxWalkNodes)
+    fail(NBGB_ERR_OVERFLOW, "Barnes-Hut node capacity above 2^30 nodes: too many bodies in one tree build");
   Node* nodes = grow(h.nodes, (size_t)h.cap);
   int32_t* par = grow(h.node_parent, (size_t)h.cap);
   int32_t* nch = grow(h.node_nchild, (size_t)h.cap);
