@@ -600,6 +600,13 @@ __global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __re
   }
 }
 
+// Arrival counter increment with acquire-release ordering at GPU scope.
+__device__ __forceinline__ int arrive_acq_rel(int32_t* p) {
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+
 // Leaves: mass/com as the reference's allocateLeaf + mergeParticleIntoLeaf
 // (force_barnes_hut.cu:355-389); then the last-arriving child of each node
 // computes that node from all its children in octant order (:514-538).
@@ -627,10 +634,9 @@ __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ 
     nodes[p].walk = walk_record(ip, nodes[p].geom.w, m);
     int node = parent[p];
     while (node >= 0) {
-      __threadfence();
-      const int arrived = atomicAdd(&visit[node], 1);
-      if (arrived != nchild[node] - 1) break;
-      __threadfence();
+      // release: this child's centre of mass is visible to the sibling that
+      // arrives last; acquire: the last one sees every sibling's
+      if (arrive_acq_rel(&visit[node]) != nchild[node] - 1) break;
       const int4 in = nodes[node].info;
       float tm = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
       int c = node + 1;
@@ -715,7 +721,7 @@ __device__ __forceinline__ void bh_add(float px, float py, float pz, float m, fl
 }
 
 template <bool COUNT, bool BUCKET>
-__global__ void __launch_bounds__(256) bh_walk_kernel(WalkArgs a) {
+__global__ void __launch_bounds__(256, 8) bh_walk_kernel(WalkArgs a) {
   const uint32_t total = a.nstart[a.n];
   const bool tree_ok = (int64_t)total <= a.cap;
   const int lane = threadIdx.x & 31;
