@@ -248,6 +248,7 @@ constexpr uint32_t kOSValMask = (1u << 30) - 1u;
 constexpr uint32_t kOSAgg = 1u << 30;  // tile aggregate published
 constexpr uint32_t kOSInc = 2u << 30;  // inclusive prefix published
 constexpr uint32_t kOSSpinLimit = 1u << 22;
+constexpr int kOSLookBatch = 4;
 // workspace (u32): counts [8][256] | offsets [8][256] | tile counters [8],
 // ticket | status [passes][n_tiles][256]
 constexpr int kOSCounters = 2 * kOSMaxPasses * 256;
@@ -368,23 +369,34 @@ __global__ void __launch_bounds__(kOSThreads) onesweep_pass_kernel(
   uint32_t* status = ws + kOSHeader + ((int64_t)pass * n_tiles) * 256;
   st_relaxed_u32(&status[tile * 256 + d], (tile == 0 ? kOSInc : kOSAgg) | total);
   s_loc[d] = block_excl_scan256(total, s_w);
-  // decoupled look-back over earlier tiles (bounded waits)
+  // decoupled look-back over earlier tiles (bounded waits), four
+  // predecessors' status words loaded at a time
   uint32_t excl = 0;
   if (tile > 0) {
-    for (int64_t t = tile - 1; t >= 0; --t) {
-      const uint32_t* sp = &status[t * 256 + d];
-      uint32_t sv = ld_relaxed_u32(sp);
-      uint32_t spins = 0;
-      while ((sv & ~kOSValMask) == 0u && ++spins < kOSSpinLimit) {
-        if (spins > 32) __nanosleep(64);
-        sv = ld_relaxed_u32(sp);
+    bool done = false;
+    for (int64_t t = tile - 1; t >= 0 && !done; t -= kOSLookBatch) {
+      uint32_t v[kOSLookBatch];
+#pragma unroll
+      for (int i = 0; i < kOSLookBatch; ++i)
+        v[i] = (t - i >= 0) ? ld_relaxed_u32(&status[(t - i) * 256 + d]) : 0u;
+#pragma unroll
+      for (int i = 0; i < kOSLookBatch; ++i) {
+        if (done || t - i < 0) break;
+        const uint32_t* sp = &status[(t - i) * 256 + d];
+        uint32_t sv = v[i];
+        uint32_t spins = 0;
+        while ((sv & ~kOSValMask) == 0u && ++spins < kOSSpinLimit) {
+          if (spins > 32) __nanosleep(64);
+          sv = ld_relaxed_u32(sp);
+        }
+        if ((sv & ~kOSValMask) == 0u) {
+          raise_error(err, kErrWaitTimeout);
+          done = true;
+          break;
+        }
+        excl += sv & kOSValMask;
+        if ((sv & ~kOSValMask) == kOSInc) done = true;
       }
-      if ((sv & ~kOSValMask) == 0u) {
-        raise_error(err, kErrWaitTimeout);
-        break;
-      }
-      excl += sv & kOSValMask;
-      if ((sv & ~kOSValMask) == kOSInc) break;
     }
     st_relaxed_u32(&status[tile * 256 + d], kOSInc | ((excl + total) & kOSValMask));
   }
