@@ -96,9 +96,21 @@ def test_keys_with_duplicates_are_stable(nb, orc):
 
 
 @pytest.mark.parametrize("gen,n,theta", [("plummer", 4096, 0.5), ("plummer", 20000, 0.3),
-                                         ("two", 50000, 0.5), ("plummer", 3000, 1.0)])
+                                         ("two", 50000, 0.5), ("plummer", 3000, 1.0),
+                                         ("far", 6000, 0.5), ("dense", 6000, 0.5)])
 def test_interaction_sets_and_forces_match_oracle_walk(nb, orc, gen, n, theta):
-    s = nb.ics.plummer(n, seed=n) if gen == "plummer" else nb.ics.two_plummer(n, seed=3)
+    """Interaction sets per target equal the oracle's (which tests cube
+    containment at every node); 'far' is a cluster 2000 units from the
+    origin (coordinate rounding comparable to the cells), 'dense' a cluster
+    whose cells shrink below the softening length."""
+    if gen == "plummer":
+        s = nb.ics.plummer(n, seed=n)
+    elif gen == "two":
+        s = nb.ics.two_plummer(n, seed=3)
+    elif gen == "far":
+        s = nb.ics.plummer(n, seed=11, center=(2000.0, -1500.0, 700.0))
+    else:
+        s = nb.ics.plummer(n, seed=12, a=0.01)
     _, _, nodes, _, merges = _oracle_tree(orc, s)
     assert merges == 0
     r = _bh(nb, s, theta=theta)
