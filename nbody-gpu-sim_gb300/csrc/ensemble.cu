@@ -833,7 +833,11 @@ nbgb_status nbgb_ensemble_create(const nbgb_ensemble_config* cfg, nbgb_ensemble*
     e->cfg = c;
     NBGB_CUDA(cudaGetDevice(&e->device));
     NBGB_CUDA(cudaStreamCreateWithFlags(&e->main, cudaStreamNonBlocking));
-    NBGB_CUDA(cudaStreamCreateWithFlags(&e->bh_stream, cudaStreamNonBlocking));
+    // the Barnes-Hut chain (build, then walk) is the tick's critical path:
+    // its blocks are scheduled ahead of the direct work queue's
+    int prio_lo = 0, prio_hi = 0;
+    NBGB_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+    NBGB_CUDA(cudaStreamCreateWithPriority(&e->bh_stream, cudaStreamNonBlocking, prio_hi));
     // arena: a quarter of the budget holds body state; the rest is for trees
     e->cap = std::max<int64_t>(kChunk, (int64_t)(c.hbm_budget_bytes / 4 / arena_bytes_per_body()) / kChunk * kChunk);
     e->x.ensure((size_t)e->cap);
