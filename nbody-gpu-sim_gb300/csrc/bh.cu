@@ -663,6 +663,11 @@ __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ 
 
 // ----------------------------------------------------------------- walk --
 // Centre of mass and cube of a node in one 256-bit load (read-only path).
+__device__ __forceinline__ void ld_node2(const Node* p, f2& cm_xy, f2& cm_zw, f2& g_xy, f2& g_zw) {
+  asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];"
+      : "=l"(cm_xy.v), "=l"(cm_zw.v), "=l"(g_xy.v), "=l"(g_zw.v)
+      : "l"(p));
+}
 __device__ __forceinline__ void ld_node(const Node* p, float4& cm, float4& g) {
   asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
       : "=f"(cm.x), "=f"(cm.y), "=f"(cm.z), "=f"(cm.w), "=f"(g.x), "=f"(g.y), "=f"(g.z), "=f"(g.w)
@@ -721,7 +726,7 @@ __device__ __forceinline__ void bh_add(float px, float py, float pz, float m, fl
 }
 
 template <bool COUNT, bool BUCKET>
-__global__ void __launch_bounds__(256, 8) bh_walk_kernel(WalkArgs a) {
+__global__ void __launch_bounds__(256, BUCKET ? 6 : (COUNT ? 7 : 8)) bh_walk_kernel(WalkArgs a) {
   const uint32_t total = a.nstart[a.n];
   const bool tree_ok = (int64_t)total <= a.cap;
   const int lane = threadIdx.x & 31;
@@ -736,16 +741,25 @@ __global__ void __launch_bounds__(256, 8) bh_walk_kernel(WalkArgs a) {
     const int64_t k = task.first + lane;
     const bool valid = k < task.end;
     const float4 pi = valid ? a.spm[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const f2 pi_xy = f2_make(pi.x, pi.y);
     float sx = 0.f, sy = 0.f, sz = 0.f;
     int cnt = 0;
     int resume = valid ? 0 : 0x7fffffff;
     int node = tree_ok ? a.seg_root[task.seg] : 0;
     const int node_end = tree_ok ? a.seg_end[task.seg] : 0;
     while (node < node_end) {
-      // one 32-byte load (centre of mass + cube), one 8-byte load (skip and
-      // flags, size2)
+      // one 32-byte load (centre of mass + cube) as four x/y, z/w pairs, one
+      // 8-byte load (skip and flags, size2); x and y differences are taken
+      // as packed FP32x2 (same IEEE rounding per component)
+      f2 cm_xy, cm_zw, g_xy, g_zw;
+      ld_node2(&a.nodes[node], cm_xy, cm_zw, g_xy, g_zw);
       float4 cm, g;
-      ld_node(&a.nodes[node], cm, g);
+      f2_split(cm_xy, cm.x, cm.y);
+      f2_split(cm_zw, cm.z, cm.w);
+      f2_split(g_xy, g.x, g.y);
+      f2_split(g_zw, g.z, g.w);
+      float tx, ty;  // target minus cube centre
+      f2_split(f2_sub(pi_xy, g_xy), tx, ty);
       const int2 wr = __ldg(&a.nodes[node].walk);
       const int skip = wr.x & (int)(kWalkZero - 1u);
       if ((uint32_t)wr.x >= kWalkZero) {  // a leaf, or zero mass
@@ -757,8 +771,7 @@ __global__ void __launch_bounds__(256, 8) bh_walk_kernel(WalkArgs a) {
         if (node >= resume) {
           float me = cm.w, cx = cm.x, cy = cm.y, cz = cm.z;
           bool use = true;
-          if (fabsf(__fsub_rn(pi.x, g.x)) <= g.w && fabsf(__fsub_rn(pi.y, g.y)) <= g.w &&
-              fabsf(__fsub_rn(pi.z, g.z)) <= g.w) {
+          if (fabsf(tx) <= g.w && fabsf(ty) <= g.w && fabsf(__fsub_rn(pi.z, g.z)) <= g.w) {
             me = __fsub_rn(cm.w, pi.w);
             use = me > 0.0f;
             if (use) {
@@ -777,11 +790,11 @@ __global__ void __launch_bounds__(256, 8) bh_walk_kernel(WalkArgs a) {
       }
       // internal node (force_barnes_hut.cu:205-243)
       const bool active = node >= resume;
-      const bool contains = fabsf(__fsub_rn(pi.x, g.x)) <= g.w &&
-                            fabsf(__fsub_rn(pi.y, g.y)) <= g.w &&
-                            fabsf(__fsub_rn(pi.z, g.z)) <= g.w;
-      const float dx = __fsub_rn(cm.x, pi.x), dy = __fsub_rn(cm.y, pi.y),
-                  dz = __fsub_rn(cm.z, pi.z);
+      const bool contains =
+          fabsf(tx) <= g.w && fabsf(ty) <= g.w && fabsf(__fsub_rn(pi.z, g.z)) <= g.w;
+      float dx, dy;
+      f2_split(f2_sub(cm_xy, pi_xy), dx, dy);
+      const float dz = __fsub_rn(cm.z, pi.z);
       const float d2 = __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), a.eps2);
       const float size2 = __int_as_float(wr.y);
       const bool accept = !contains && opening_accept(size2, d2, a.th_lo, a.th_hi, a.theta2);

@@ -127,11 +127,12 @@ __global__ void __launch_bounds__(256) hash_force_kernel(
       for (int oy = -1; oy <= 1; ++oy) {
         const int ny = cy + oy;
         if (ny < 0 || ny >= g.dims[1]) continue;
-        for (int ox = -1; ox <= 1; ++ox) {
-          const int nx = cx + ox;
-          if (nx < 0 || nx >= g.dims[0]) continue;
-          const int c = nx + ny * g.dims[0] + nz * gxy;
-          const uint32_t s = start[c], e = start[c + 1];
+        {
+          // cells cx-1 .. cx+1 of this row are consecutive in the sorted
+          // array: one range, in the reference's cell order
+          const int row = ny * g.dims[0] + nz * gxy;
+          const uint32_t s = start[row + max(cx - 1, 0)];
+          const uint32_t e = start[row + min(cx + 1, g.dims[0] - 1) + 1];
           for (uint32_t j = s; j < e; ++j) {
             if ((int64_t)j == k) continue;
             const float4 pj = spm[j];
