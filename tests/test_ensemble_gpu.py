@@ -195,3 +195,36 @@ def _calc_bh(nb, pos, m, theta=0.5, eps=0.01):
         acc = (p.host["acc_x"].copy(), p.host["acc_y"].copy(), p.host["acc_z"].copy())
     calc.close()
     return acc
+
+
+def test_batched_bh_many_segments_degenerate(nb):
+    """300 Barnes-Hut systems in one batched pass (a two-digit segment sort),
+    among them coincident bodies (depth-32 leaves), zero-mass bodies (skipped
+    subtrees) and single bodies: each equals the single-system calculator
+    bit for bit."""
+    from nbgb.serving import Ensemble
+    ens = Ensemble(direct_max_n=0, max_resident=400, hbm_budget_bytes=2 << 30)
+    reqs = {}
+    for i in range(300):
+        n = 1 + (i * 7) % 40
+        s = nb.ics.plummer(n, seed=100 + i)
+        if i % 5 == 1 and n > 3:
+            for k in ("x", "y", "z", "vx", "vy", "vz"):
+                s[k][: n // 2] = s[k][0]  # a coincident half that stays coincident
+        if i % 5 == 2 and n > 3:
+            s["m"][::2] = 0.0  # zero-mass bodies
+        reqs[ens.submit(s, 2, 1e-3)] = n
+    for _ in range(20):
+        if ens.tick() == (0, 0):
+            break
+    ens.synchronize()
+    got = {}
+    while (r := ens.poll(want_state=True, want_acc=True)) is not None:
+        got[r[0]["request_id"]] = r[1]
+    ens.close()
+    assert len(got) == len(reqs)
+    for rid, s in got.items():
+        pos = {k: s[k].astype(np.float32) for k in ("x", "y", "z")}
+        ref = _calc_bh(nb, pos, s["m"])
+        for k, a in zip(("ax", "ay", "az"), ref):
+            np.testing.assert_array_equal(s[k], a, err_msg=f"request {rid} n={reqs[rid]} {k}")
