@@ -34,17 +34,18 @@ def _torchrun(script: str, *args, timeout=300):
 def test_reduce_over_ranks_gloo(tmp_path):
     script = tmp_path / "ranks.py"
     script.write_text(
-        "import json, os\n"
+        "import json, os, sys\n"
         "import torch.distributed as dist\n"
         "import bench\n"
         "dist.init_process_group('gloo')\n"
         "r, w = dist.get_rank(), dist.get_world_size()\n"
         "t, ps = bench.reduce_over_ranks(1.0 + r, 100.0 * (r + 1), w)\n"
-        "print(json.dumps({'rank': r, 't': t, 'ps': ps, 'seed': bench.shard_seed(r)}), flush=True)\n"
+        "out = os.path.join(sys.argv[1], f'rank{r}.json')\n"
+        "open(out, 'w').write(json.dumps({'rank': r, 't': t, 'ps': ps, 'seed': bench.shard_seed(r)}))\n"
         "dist.destroy_process_group()\n")
-    res = _torchrun(str(script))
+    res = _torchrun(str(script), str(tmp_path))
     assert res.returncode == 0, res.stderr[-2000:]
-    lines = [json.loads(l) for l in res.stdout.splitlines() if l.startswith("{")]
+    lines = [json.loads((tmp_path / f"rank{r}.json").read_text()) for r in range(2)]
     assert sorted(d["rank"] for d in lines) == [0, 1]
     for d in lines:
         assert d["t"] == 2.0 and d["ps"] == 300.0  # max of elapsed, sum of work
