@@ -110,7 +110,6 @@ struct BHState {
   DevBuf<Node> nodes;
   DevBuf<int32_t> node_parent, node_nchild, node_visit;
   DevBuf<float4> spm;      // bodies in path order
-  DevBuf<unsigned long long> inter_total;
   DevBuf<uint32_t> walk_ctr;  // next warp task of the walk
   int64_t n = 0;
   int64_t reserve = 0;  // bodies the per-body buffers are sized for (>= n)
@@ -662,15 +661,11 @@ __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ 
 }
 
 // ----------------------------------------------------------------- walk --
-// Centre of mass and cube of a node in one 256-bit load (read-only path).
+// Centre of mass and cube of a node in one 256-bit load (read-only path),
+// as the register pairs (com x, y), (com z, mass), (centre x, y), (centre z, half).
 __device__ __forceinline__ void ld_node2(const Node* p, f2& cm_xy, f2& cm_zw, f2& g_xy, f2& g_zw) {
   asm("ld.global.nc.v4.b64 {%0, %1, %2, %3}, [%4];"
       : "=l"(cm_xy.v), "=l"(cm_zw.v), "=l"(g_xy.v), "=l"(g_zw.v)
-      : "l"(p));
-}
-__device__ __forceinline__ void ld_node(const Node* p, float4& cm, float4& g) {
-  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-      : "=f"(cm.x), "=f"(cm.y), "=f"(cm.z), "=f"(cm.w), "=f"(g.x), "=f"(g.y), "=f"(g.z), "=f"(g.w)
       : "l"(p));
 }
 
@@ -858,7 +853,7 @@ size_t bh_state_bytes(const BHState* p) {
          h.hist.bytes() + h.scan_ws.bytes() + h.lcp.bytes() + h.ncnt.bytes() + h.nstart.bytes() +
          h.scalars.bytes() + h.nodes.bytes() +
          h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() + h.spm.bytes() +
-         h.inter_total.bytes() + h.walk_ctr.bytes();
+         h.walk_ctr.bytes();
 }
 
 size_t bh_bytes_estimate(int64_t n) { return (size_t)n * 480 + (64u << 10); }
