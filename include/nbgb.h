@@ -179,6 +179,44 @@ nbgb_status nbgb_particles_copy_to_device(nbgb_particle_data* d, const nbgb_part
 nbgb_status nbgb_particles_copy_to_host(nbgb_particle_data* h, const nbgb_particle_data* d);
 
 /* ---------------------------------------------------------------------------
+ * Initial conditions generated on the device (ParticleInitializer::initUniform
+ * / initSpherical / initDisk, src/cuda/particle_init.cu:167-234, generate on
+ * the host; these write straight into device arrays).  Same formulas as the
+ * reference plus a Plummer sphere; the random stream is a counter-based
+ * generator (deterministic per seed, independent of the launch shape), not
+ * the reference's std::mt19937 sequence.  acc and acc_old are zeroed.
+ * Synchronous on `stream`.
+ * ------------------------------------------------------------------------- */
+typedef enum nbgb_distribution {
+  NBGB_DIST_UNIFORM = 0,
+  NBGB_DIST_SPHERICAL = 1,
+  NBGB_DIST_DISK = 2,
+  NBGB_DIST_PLUMMER = 3
+} nbgb_distribution;
+
+typedef struct nbgb_init_params {
+  int32_t distribution;   /* nbgb_distribution */
+  float center[3];        /* spherical, disk, Plummer */
+  float radius;           /* spherical, disk */
+  float min_bounds[3];    /* uniform */
+  float max_bounds[3];
+  float min_mass;         /* uniform, spherical, disk: mass uniform in [min, max] */
+  float max_mass;
+  float thickness;        /* disk */
+  float rotation_speed;   /* disk: v = rotation_speed * sqrt(r) */
+  float plummer_a;        /* Plummer scale radius, total mass, G (equal masses M/N) */
+  float total_mass;
+  float G;
+} nbgb_init_params;
+
+/* Parameters ParticleSystem::initialize uses (particle_system.cpp:77-101):
+ * box [-10, 10]^3, ball / disk radius 10, thickness 1, rotation 0.5, mass 1;
+ * Plummer a = 1, M = 1, G = 1. */
+void nbgb_init_params_default(nbgb_init_params* p, int32_t distribution);
+nbgb_status nbgb_init_particles_device(nbgb_particle_data* d_particles, const nbgb_init_params* p,
+                                       uint64_t seed, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Inspection for parity tests: what the reference exposes through
  * BarnesHutTree (include/nbody/barnes_hut_tree.hpp:38-91) and SpatialHashGrid
  * (include/nbody/spatial_hash_grid.hpp:9-62).  Host output buffers; each call

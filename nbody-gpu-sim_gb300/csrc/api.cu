@@ -12,7 +12,7 @@ namespace nbgb {
 
 static thread_local std::string g_last_error;
 
-static nbgb_status set_error(nbgb_status s, const std::string& msg) {
+nbgb_status set_error(nbgb_status s, const std::string& msg) {
   g_last_error = msg;
   return s;
 }

@@ -783,7 +783,6 @@ static void run_tick(nbgb_ensemble* e) {
 
 }  // namespace nbgb
 
-static thread_local std::string g_ens_err;
 
 template <typename F>
 static nbgb_status ens_guard(F&& f) {
@@ -791,7 +790,7 @@ static nbgb_status ens_guard(F&& f) {
     f();
     return NBGB_OK;
   } catch (const Error& err) {
-    g_ens_err = err.what();
+    set_error(err.status, err.what());
     return err.status;
   } catch (const std::bad_alloc&) {
     return NBGB_ERR_OOM;
@@ -964,7 +963,7 @@ nbgb_status nbgb_ensemble_poll(nbgb_ensemble* e, nbgb_ensemble_result* result,
   cudaEventDestroy(r.evt);
   e->retiring.pop_front();
   if (bits) {
-    g_ens_err = "device error word set during the ensemble run";
+    set_error(NBGB_ERR_OVERFLOW, "device error word set during the ensemble run");
     return bits & kErrWaitTimeout ? NBGB_ERR_DEVICE_TIMEOUT : NBGB_ERR_OVERFLOW;
   }
   return NBGB_OK;

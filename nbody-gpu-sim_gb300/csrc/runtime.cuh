@@ -113,5 +113,7 @@ void hash_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, flo
 int64_t direct_pad(int64_t n);
 // Wait for the calculator's stream and turn device error bits into an Error.
 void check_device_errors(nbgb_calculator* c);
+// Record msg as this thread's nbgb_last_error() text; returns s.
+nbgb_status set_error(nbgb_status s, const std::string& msg);
 
 }  // namespace nbgb

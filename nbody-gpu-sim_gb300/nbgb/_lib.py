@@ -34,6 +34,17 @@ class OctreeNode(C.Structure):
                 ("is_leaf", C.c_uint8), ("pad_", C.c_uint8 * 3), ("particle_count", C.c_int32)]
 
 
+class InitParams(C.Structure):
+    _fields_ = [("distribution", C.c_int32), ("center", C.c_float * 3), ("radius", C.c_float),
+                ("min_bounds", C.c_float * 3), ("max_bounds", C.c_float * 3),
+                ("min_mass", C.c_float), ("max_mass", C.c_float), ("thickness", C.c_float),
+                ("rotation_speed", C.c_float), ("plummer_a", C.c_float),
+                ("total_mass", C.c_float), ("G", C.c_float)]
+
+
+DIST_UNIFORM, DIST_SPHERICAL, DIST_DISK, DIST_PLUMMER = 0, 1, 2, 3
+
+
 class EnsembleConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_resident", C.c_int32),
                 ("direct_max_n", C.c_int32), ("G", C.c_float), ("softening", C.c_float),
@@ -93,6 +104,8 @@ _SIGS = {
     "nbgb_particles_free_device": (C.c_int, [_pd]),
     "nbgb_particles_copy_to_device": (C.c_int, [_pd, _pd]),
     "nbgb_particles_copy_to_host": (C.c_int, [_pd, _pd]),
+    "nbgb_init_params_default": (None, [C.POINTER(InitParams), C.c_int32]),
+    "nbgb_init_particles_device": (C.c_int, [_pd, C.POINTER(InitParams), C.c_uint64, _vp]),
     "nbgb_bh_tree_stats": (C.c_int, [_vp, _i32p, _i32p]),
     "nbgb_bh_copy_sorted_keys": (C.c_int, [_vp, _vp, _vp, C.c_size_t]),
     "nbgb_bh_copy_nodes": (C.c_int, [_vp, _vp, C.c_size_t]),

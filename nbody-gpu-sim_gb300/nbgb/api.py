@@ -142,6 +142,23 @@ class ParticleDataManager:
     def copyToHost(h: ParticleData, d: ParticleData) -> None:  # noqa: N802
         check(_lib.lib().nbgb_particles_copy_to_host(h.ptr(), d.ptr()))
 
+    @staticmethod
+    def initDevice(d: ParticleData, distribution: int, seed: int = 42,  # noqa: N802
+                   **params) -> None:
+        """Initial conditions generated in the device arrays of d
+        (nbgb_init_particles_device); params override the defaults of
+        nbgb_init_params_default (center, radius, min_bounds, max_bounds,
+        min_mass, max_mass, thickness, rotation_speed, plummer_a,
+        total_mass, G)."""
+        p = _lib.InitParams()
+        _lib.lib().nbgb_init_params_default(C.byref(p), distribution)
+        for k, v in params.items():
+            if k in ("center", "min_bounds", "max_bounds"):
+                getattr(p, k)[:] = [float(x) for x in v]
+            else:
+                setattr(p, k, v)
+        check(_lib.lib().nbgb_init_particles_device(d.ptr(), C.byref(p), seed, None))
+
 
 class ScopedParticleData:
     """Device + host pair, like tests/particle_data_fixture.hpp:11-27."""
