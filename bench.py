@@ -304,6 +304,7 @@ def gpu_arm(args, rank, world, local):
                              h2d=h2d, d2h=d2h)
         # --- CPU baseline (reference CPU path, restated) -------------------------
         cpu = cpu_baseline(nbgb, stream, args.cpu_seconds)
+        force_err = measured_force_error(nbgb)
 
         ffma_peak = ffma.value
         d_achieved = 20.0 * dint / (dms / 1e3) / 1e12 if dms > 0 else None
@@ -328,9 +329,11 @@ def gpu_arm(args, rank, world, local):
                 "direct_kernel_config": tuned, "theta": 0.5, "softening": EPS, "dt": DT,
                 "force_error": "direct: compensated FP32, median rel err ~1e-7 vs FP64; "
                                "Barnes-Hut theta=0.5: median rel err <= 2e-3 vs FP64 "
-                               "(tests/test_bh_gpu.py, tests/test_direct_gpu.py)",
+                               "(tests/test_bh_gpu.py, tests/test_direct_gpu.py); measured "
+                               "on served systems: force_error_measured",
                 "parallelism": f"replicas x{world} (request-stream shards)",
             },
+            "force_error_measured": force_err,
             "batched_particle_steps_per_s": value,
             "plain_particle_steps_per_s": plain["value"] if plain else None,
             "batched_vs_plain": (value / world / plain["value"]) if plain else None,
@@ -373,6 +376,47 @@ def gpu_arm(args, rank, world, local):
             "clocks": clocks,
             "gpu_launches": launches,
         }
+    return out
+
+
+def measured_force_error(nbgb) -> dict:
+    """Force error of the ensemble's accelerations as served: one direct
+    (N = 6000) and one Barnes-Hut (N = 30000) system of the serving workload
+    run 3 steps in one engine; their final accelerations are compared with
+    the FP64 direct sum at the final FP32 positions (nbgb_direct_f64) on
+    2048 seeded targets each (vector relative error)."""
+    import ctypes as C
+
+    import torch
+
+    from nbgb.serving import Ensemble
+    ens = Ensemble(hbm_budget_bytes=4 << 30, softening=EPS, theta=0.5)
+    sys_ = {ens.submit(nbgb.ics.plummer(6000, seed=901), 3, DT): "direct",
+            ens.submit(nbgb.ics.plummer(30000, seed=902), 3, DT): "barnes_hut"}
+    for _ in range(20):
+        if ens.tick() == (0, 0):
+            break
+    ens.synchronize()
+    out = {}
+    while (r := ens.poll(want_state=True, want_acc=True)) is not None:
+        s = r[1]
+        n = len(s["m"])
+        xyzm = np.stack([s["x"].astype(np.float32), s["y"].astype(np.float32),
+                         s["z"].astype(np.float32), s["m"]], 1)
+        src = torch.from_numpy(np.ascontiguousarray(xyzm)).cuda()
+        tg = np.sort(np.random.default_rng(n).choice(n, 2048, replace=False)).astype(np.int64)
+        tgd = torch.from_numpy(tg).cuda()
+        acc = [torch.empty(len(tg), dtype=torch.float64, device="cuda") for _ in range(3)]
+        nbgb.check(nbgb.lib().nbgb_direct_f64(C.c_void_p(src.data_ptr()), n,
+                                               C.c_void_p(tgd.data_ptr()), len(tg), 1.0, EPS,
+                                               *(C.c_void_p(a.data_ptr()) for a in acc), None))
+        torch.cuda.synchronize()
+        ref = np.stack([a.cpu().numpy() for a in acc], 1)
+        got = np.stack([s["ax"][tg], s["ay"][tg], s["az"][tg]], 1).astype(np.float64)
+        e = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        out[sys_[r[0]["request_id"]]] = {"n": n, "median": float(np.median(e)),
+                                         "p99": float(np.quantile(e, 0.99))}
+    ens.close()
     return out
 
 
