@@ -384,6 +384,13 @@ nbgb_status nbgb_direct_f64(const float* d_src_xyzm, int64_t n_src, const int64_
  * ------------------------------------------------------------------------- */
 nbgb_status nbgb_measure_fp32_peak(double* ffma_tflops, double* ffma2_tflops, double* mufu_gops);
 
+/* Failure-detection self-test (no reference counterpart): one thread waits,
+ * through the kernels' own bounded mbarrier wait, on a barrier nothing
+ * arrives at, giving up after max_iters tries (1 .. 2^20).  Returns
+ * NBGB_ERR_DEVICE_TIMEOUT with the device error bits in *error_bits; the
+ * context stays usable.  Nothing faults, traps or hangs. */
+nbgb_status nbgb_selftest_wait_timeout(uint32_t max_iters, uint32_t* error_bits);
+
 /* ---------------------------------------------------------------------------
  * Library information.
  * ------------------------------------------------------------------------- */
