@@ -421,7 +421,9 @@ def measured_force_error(nbgb) -> dict:
 
 
 def plain_arm(nbgb, reqs, steps) -> dict:
-    """Each request alone through the plain device path, in sequence."""
+    """Each request alone through the plain device path, in sequence: the
+    device-resident FP64 system with asynchronous calculators (no per-step
+    host synchronisation; one at the end)."""
     tot_ps, tot_s = 0.0, 0.0
     per = []
     for r in reqs:
@@ -431,10 +433,13 @@ def plain_arm(nbgb, reqs, steps) -> dict:
         else:
             calc = nbgb.BarnesHutCalculator(0.5)
         calc.setSofteningParameter(EPS)
+        calc.set_flags(nbgb.FLAG_COMPENSATED)  # asynchronous: no per-step read-back
         sysm = nbgb.System(calc, s)
         sysm.step(DT, 2)  # warm
+        calc.synchronize()
         t0 = time.perf_counter()
-        sysm.step(DT, steps)  # synchronizes at the end
+        sysm.step(DT, steps)
+        calc.synchronize()
         dt = time.perf_counter() - t0
         sysm.close()
         calc.close()
