@@ -56,8 +56,8 @@ def parse():
     ap.add_argument("--resident", type=int, default=96, help="resident systems at saturation")
     ap.add_argument("--plain-requests", type=int, default=48)
     ap.add_argument("--plain-steps", type=int, default=20)
-    ap.add_argument("--serve-requests", type=int, default=192)
-    ap.add_argument("--serve-max-s", type=float, default=90.0)
+    ap.add_argument("--serve-requests", type=int, default=384)
+    ap.add_argument("--serve-max-s", type=float, default=120.0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-budget-s", type=float, default=120.0,
                     help="--impl reference: CPU seconds spread over warmup + steps")
