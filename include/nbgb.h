@@ -283,8 +283,9 @@ nbgb_status nbgb_system_read(nbgb_system* sys, nbgb_particle_data* h_out);
 nbgb_status nbgb_system_read_f64(nbgb_system* sys, double* x, double* y, double* z, double* vx,
                                  double* vy, double* vz);
 /* FP64 energy and momentum from the FP64 state: KE = sum m v^2/2, PE =
- * -sum_{i<j} G m_i m_j / sqrt(r^2 + eps^2) (integrator.cu:52-120; here in
- * FP64 arithmetic, O(N^2)), P = sum m v. */
+ * -sum_{i<j} G m_i m_j / sqrt(r^2 + eps^2) (integrator.cu:52-120; O(N^2), in
+ * FP64 arithmetic up to 2^18 bodies, above that FP32 pair terms with FP64
+ * accumulation), P = sum m v. */
 nbgb_status nbgb_system_energy(nbgb_system* sys, double* ke, double* pe, double momentum[3]);
 
 /* ---------------------------------------------------------------------------

@@ -171,6 +171,8 @@ using namespace nbgb;
 // ---------------------------------------------------------------------------
 // Device-resident FP64 system.
 // ---------------------------------------------------------------------------
+constexpr int64_t kPotentialF64MaxN = (int64_t)1 << 18;
+
 struct nbgb_system {
   nbgb_calculator* calc = nullptr;
   int64_t n = 0;
@@ -633,10 +635,18 @@ nbgb_status nbgb_system_energy(nbgb_system* s, double* ke, double* pe, double mo
     double kin[4] = {h[0], h[1], h[2], h[3]};
     double pot = 0.0;
     if (pe) {
-      // FP64 positions, FP64 arithmetic (the state the system integrates)
-      const double eps = (double)c->params.softening;
-      launch_potential_f64(s->x.ptr, s->y.ptr, s->z.ptr, s->pm.ptr, s->n, eps * eps, p, nb,
-                           p + (size_t)nb * 4, st);
+      // FP64 positions and arithmetic (the state the system integrates) up
+      // to 2^18 bodies; above, the O(N^2) FP64 sum would take seconds on
+      // GB300's FP64 pipe, so the FP32 pair terms (Newton-refined rsqrt,
+      // compensated per tile, FP64 totals) are summed instead
+      if (s->n <= kPotentialF64MaxN) {
+        const double eps = (double)c->params.softening;
+        launch_potential_f64(s->x.ptr, s->y.ptr, s->z.ptr, s->pm.ptr, s->n, eps * eps, p, nb,
+                             p + (size_t)nb * 4, st);
+      } else {
+        const float eps = c->params.softening;
+        launch_potential(s->pm.ptr, s->n, eps * eps, p, nb, p + (size_t)nb * 4, st);
+      }
       NBGB_CUDA(cudaMemcpyAsync(h, p + (size_t)nb * 4, sizeof(double), cudaMemcpyDeviceToHost, st));
       NBGB_CUDA(cudaStreamSynchronize(st));
       pot = (double)c->params.G * h[0];
