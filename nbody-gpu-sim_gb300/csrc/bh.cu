@@ -65,8 +65,8 @@ struct __align__(16) Node {
   float4 geom;  // cube centre, half size
   int4 info;    // skip (next node outside the subtree), depth << 8 | leaf,
                 // first body, body count
-  int2 walk;    // for the walk: skip | leaf << 31 | zero mass << 30, bits of 4 h^2
-  int2 pad;
+  int4 walk;    // for the walk: skip | leaf << 31 | zero mass << 30, bits of 4 h^2,
+                // first body, body count
 };
 
 constexpr uint32_t kWalkLeaf = 1u << 31;
@@ -76,11 +76,11 @@ constexpr int64_t kMaxWalkNodes = (int64_t)1 << 30;  // skip indices below the f
 // The walk record of a node whose centre of mass is final: skip and flags,
 // and the opening test's size2 = 4 h^2 (force_barnes_hut.cu:222) rounded as
 // the reference rounds it.
-__device__ __forceinline__ int2 walk_record(const int4& in, float h, float mass) {
+__device__ __forceinline__ int4 walk_record(const int4& in, float h, float mass) {
   uint32_t w = (uint32_t)in.x;
   if (in.y & 1) w |= kWalkLeaf;
   if (mass == 0.0f) w |= kWalkZero;
-  return make_int2((int)w, __float_as_int(__fmul_rn(__fmul_rn(4.0f, h), h)));
+  return make_int4((int)w, __float_as_int(__fmul_rn(__fmul_rn(4.0f, h), h)), in.z, in.w);
 }
 
 struct BHState {
@@ -755,7 +755,14 @@ __global__ void __launch_bounds__(256, BUCKET ? 6 : (COUNT ? 7 : 8)) bh_walk_ker
       f2_split(g_zw, g.z, g.w);
       float tx, ty;  // target minus cube centre
       f2_split(f2_sub(pi_xy, g_xy), tx, ty);
-      const int2 wr = __ldg(&a.nodes[node].walk);
+      // the bucket walk also needs the node's body range (same 16-byte load)
+      int4 wr;
+      if (BUCKET) {
+        wr = __ldg(&a.nodes[node].walk);
+      } else {
+        const int2 w2 = __ldg(reinterpret_cast<const int2*>(&a.nodes[node].walk));
+        wr = make_int4(w2.x, w2.y, 0, 0);
+      }
       const int skip = wr.x & (int)(kWalkZero - 1u);
       if ((uint32_t)wr.x >= kWalkZero) {  // a leaf, or zero mass
         if ((uint32_t)wr.x & kWalkZero) {  // force_barnes_hut.cu:172-173
@@ -803,21 +810,21 @@ __global__ void __launch_bounds__(256, BUCKET ? 6 : (COUNT ? 7 : 8)) bh_walk_ker
         if (COUNT) ++cnt;
         resume = skip;
       }
-      if (BUCKET) {
-        const int4 full = a.nodes[node].info;  // first, count
-        if (full.w <= a.leaf_cap) {
-          if (open) {
-            for (int j = 0; j < full.w; ++j) {
-              const int64_t s = (int64_t)full.z + j;
-              if (s == k) continue;
-              const float4 q = a.spm[s];
+      if (BUCKET && wr.w <= a.leaf_cap) {
+        // a subtree of at most leaf_cap bodies: the lanes that open it sum
+        // its bodies directly (all read the same body: one broadcast load)
+        if (open) {
+          const int64_t self = k - wr.z;
+          for (int j = 0; j < wr.w; ++j) {
+            const float4 q = __ldg(&a.spm[wr.z + j]);
+            if (j != self) {
               bh_add(q.x, q.y, q.z, q.w, pi.x, pi.y, pi.z, a.eps2, sx, sy, sz);
               if (COUNT) ++cnt;
             }
           }
-          node = skip;
-          continue;
         }
+        node = skip;
+        continue;
       }
       node = __any_sync(0xffffffffu, open) ? node + 1 : skip;
     }

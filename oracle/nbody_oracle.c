@@ -490,14 +490,23 @@ int orc_build_octree(int64_t n, const float* x, const float* y, const float* z, 
  * (:218-224), stack guard sp+8 <= 256 (:234).  rsqrtf is replaced by
  * 1/sqrtf on the CPU; the opening test uses the contracted distance
  * expression shared with the CUDA walk (see file header).  Optionally
- * reports the number of accepted interactions per target. */
-void orc_bh_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* x,
-                   const float* y, const float* z, const float* m, float theta, float G,
-                   float eps, const int64_t* targets, int64_t n_targets, float* ax, float* ay,
-                   float* az, int32_t* interactions) {
+ * reports the number of accepted interactions per target.
+ *
+ * leaf_cap > 1 walks the same tree with every subtree of at most leaf_cap
+ * bodies collapsed into one bucket (the bucket variant of the reference
+ * walk; the reference itself has leaf_cap 1): an internal bucket node that
+ * fails the opening test is replaced by the direct sum over its bodies in
+ * octant order, skipping the target itself by index.  Returns ORC_ERR_ARG
+ * when a bucket holds a multi-body (depth-32) leaf, whose bodies the node
+ * records do not list. */
+int orc_bh_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* x,
+                  const float* y, const float* z, const float* m, float theta, float G,
+                  float eps, const int64_t* targets, int64_t n_targets, float* ax, float* ay,
+                  float* az, int32_t* interactions, int leaf_cap) {
   float theta2 = theta * theta;
   float eps2 = eps * eps;
-#pragma omp parallel for schedule(dynamic, 64)
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 64) reduction(| : bad)
   for (int64_t t = 0; t < n_targets; t++) {
     int64_t i = targets ? targets[t] : t;
     float xi = x[i], yi = y[i], zi = z[i], mi = m[i];
@@ -542,6 +551,32 @@ void orc_bh_forces(const orc_node* nodes, int num_nodes, int64_t n, const float*
         sy += f * dy;
         sz += f * dz;
         inter++;
+      } else if (leaf_cap > 1 && nd->particle_count <= leaf_cap) {
+        int bst[64];
+        int bp = 0;
+        bst[bp++] = ni;
+        while (bp > 0) {
+          const orc_node* b = &nodes[bst[--bp]];
+          if (!b->is_leaf) {
+            for (int c = 7; c >= 0; c--)
+              if (b->children[c] >= 0 && bp < 64) bst[bp++] = b->children[c];
+            continue;
+          }
+          if (b->particle_count != 1) {
+            bad = 1;
+            continue;
+          }
+          int64_t j = b->particle_index;
+          if (j == i) continue;
+          float ex = x[j] - xi, ey = y[j] - yi, ez = z[j] - zi;
+          float e2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex)) + eps2;
+          float inv = 1.0f / sqrtf(e2);
+          float f = G * m[j] * (inv * inv * inv);
+          sx += f * ex;
+          sy += f * ey;
+          sz += f * ez;
+          inter++;
+        }
       } else if (sp + 8 <= 256) {
         for (int c = 0; c < 8; c++)
           if (nd->children[c] >= 0) stack[sp++] = nd->children[c];
@@ -552,6 +587,7 @@ void orc_bh_forces(const orc_node* nodes, int num_nodes, int64_t n, const float*
     az[t] = sz;
     if (interactions) interactions[t] = inter;
   }
+  return bad ? ORC_ERR_ARG : ORC_OK;
 }
 
 /* ------------------------------------------------------------------------ */

@@ -71,7 +71,7 @@ class Oracle:
                                          C.POINTER(C.c_int), C.POINTER(C.c_int64)]
         lib.orc_bh_forces.argtypes = [C.c_void_p, C.c_int, _i64, _f32p, _f32p, _f32p, _f32p,
                                       _f, _f, _f, C.c_void_p, _i64, _f32p, _f32p, _f32p,
-                                      C.c_void_p]
+                                      C.c_void_p, C.c_int]
         lib.orc_hash_dims.argtypes = [_i64, _f32p, _f32p, _f32p, _f, _f32p, _f32p, _i32p,
                                       C.POINTER(C.c_int64)]
         lib.orc_hash_build.argtypes = [_i64, _f32p, _f32p, _f32p, _f, _f32p, _i32p, _i32p,
@@ -168,7 +168,7 @@ class Oracle:
             raise OverflowError("oracle octree: node array overflow")
         return nodes[: cnt.value].copy(), dep.value, merges.value
 
-    def bh_forces(self, nodes, x, y, z, m, theta, G, eps, targets=None):
+    def bh_forces(self, nodes, x, y, z, m, theta, G, eps, targets=None, leaf_cap=1):
         x, y, z, m = map(_f32, (x, y, z, m))
         nodes = np.ascontiguousarray(nodes, NODE_DTYPE)
         n = len(x)
@@ -179,8 +179,10 @@ class Oracle:
             nt, tp = len(tkeep), tkeep.ctypes.data_as(C.c_void_p)
         ax, ay, az = (np.zeros(nt, np.float32) for _ in range(3))
         inter = np.zeros(nt, np.int32)
-        self.lib.orc_bh_forces(nodes.ctypes.data, len(nodes), n, x, y, z, m, theta, G, eps, tp,
-                               nt, ax, ay, az, inter.ctypes.data)
+        rc = self.lib.orc_bh_forces(nodes.ctypes.data, len(nodes), n, x, y, z, m, theta, G, eps,
+                                    tp, nt, ax, ay, az, inter.ctypes.data, leaf_cap)
+        if rc != 0:
+            raise ValueError("oracle bucket walk: a bucket holds a multi-body leaf")
         return ax, ay, az, inter
 
     # -- spatial hash ------------------------------------------------------------

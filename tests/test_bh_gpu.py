@@ -5,10 +5,11 @@ Bit-exact: Morton keys and the stably sorted (key, index) pairs; the octree
 body, body count) against the reference's host insertion build -- golden
 node arrays produced by the reference's own code, and the oracle's
 restatement of it (pinned bit-exact to those goldens) for larger inputs;
-per-target accepted-interaction counts against the oracle walk.  Forces:
-reference semantics (one body per leaf) within 1e-5 (p99, vector relative)
-of the oracle walk on the same tree; theta = 0.5 with 8-body buckets median
-relative error <= 2e-3 against the FP64 direct sum.
+per-target accepted-interaction counts against the oracle walk (one body
+per leaf, and the bucket walk over subtrees of at most 2..16 bodies).
+Forces within 1e-5 (p99, vector relative) of the oracle walk on the same
+tree; theta = 0.5 with 8-body buckets median relative error <= 2e-3 against
+the FP64 direct sum.
 """
 from __future__ import annotations
 
@@ -123,6 +124,30 @@ def test_interaction_sets_and_forces_match_oracle_walk(nb, orc, gen, n, theta):
     assert np.percentile(err, 99) <= 1e-5, np.percentile(err, 99)
 
 
+@pytest.mark.parametrize("gen,n,theta,leaf", [("plummer", 20000, 0.5, 8), ("two", 50000, 0.5, 8),
+                                              ("plummer", 6000, 0.3, 2), ("plummer", 6000, 0.8, 16),
+                                              ("dense", 6000, 0.5, 8)])
+def test_bucket_interaction_sets_match_oracle_walk(nb, orc, gen, n, theta, leaf):
+    """Bucket walk (subtrees of at most `leaf` bodies summed directly):
+    per-target interaction counts equal the oracle's bucket walk on the same
+    tree, forces within 1e-5 (p99, vector relative)."""
+    if gen == "plummer":
+        s = nb.ics.plummer(n, seed=n + leaf)
+    elif gen == "two":
+        s = nb.ics.two_plummer(n, seed=4)
+    else:
+        s = nb.ics.plummer(n, seed=13, a=0.01)
+    _, _, nodes, _, merges = _oracle_tree(orc, s)
+    assert merges == 0
+    r = _bh(nb, s, theta=theta, leaf=leaf)
+    t = np.random.default_rng(6).choice(n, min(n, 4096), replace=False)
+    ox, oy, oz, oint = orc.bh_forces(nodes, s["x"], s["y"], s["z"], s["m"], theta, 1.0, 0.01,
+                                     targets=t, leaf_cap=leaf)
+    np.testing.assert_array_equal(r["inter"][t], oint)
+    err = vec_rel_err(*(a[t] for a in r["acc"]), ox, oy, oz)
+    assert np.percentile(err, 99) <= 1e-5, np.percentile(err, 99)
+
+
 def test_small_theta_matches_direct(nb, golden):
     # tests/test_spatial_hash.cpp:171-228: theta = 0.1 vs direct < 2 % per
     # component (the canonical tree; the reference's 2N budget merge would
@@ -213,6 +238,14 @@ def test_full_size_two_plummer(nb, orc):
     bx, by, bz = orc.direct_f64(s["x"], s["y"], s["z"], s["m"], 1.0, 0.01, targets=t)
     err = vec_rel_err(*(a[t] for a in r["acc"]), bx, by, bz)
     assert np.median(err) <= 2e-3
+    # the same workload with 8-body buckets: interaction sets equal the
+    # oracle's bucket walk on the same tree, and the same error bound
+    r8 = _bh(nb, s, theta=0.5, leaf=8)
+    _, _, _, oint = orc.bh_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.5, 1.0, 0.01,
+                                  targets=t, leaf_cap=8)
+    np.testing.assert_array_equal(r8["inter"][t], oint)
+    err8 = vec_rel_err(*(a[t] for a in r8["acc"]), bx, by, bz)
+    assert np.median(err8) <= 2e-3
     r8 = _bh(nb, s, theta=0.5, leaf=8, count=False)
     err8 = vec_rel_err(*(a[t] for a in r8["acc"]), bx, by, bz)
     assert np.median(err8) <= 2e-3

@@ -131,6 +131,34 @@ def test_bh_theta_convergence(orc, golden):
     assert total(0.3) <= 1.1 * total(0.8)
 
 
+def test_bh_bucket_walk_limits(orc, golden):
+    # The bucket walk (subtrees of at most leaf_cap bodies summed directly):
+    # leaf_cap 1 is the reference walk; a bucket as large as the system makes
+    # the root one bucket, i.e. the direct sum over every other body; theta 0
+    # opens every bucket, so every target meets every other body once.
+    g = golden("ref_inputs.npz")
+    x, y, z, m = (g[f"sph50_r10_{k}"] for k in ("x", "y", "z", "m"))
+    n = len(x)
+    bmin, bmax = orc.bbox(x, y, z)
+    _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
+    nodes, _, merges = orc.build_octree(x, y, z, m, si, bmin, bmax, max_nodes=64 * n + 64)
+    assert merges == 0
+    ref = orc.bh_forces(nodes, x, y, z, m, 0.5, 1.0, 0.1)
+    one = orc.bh_forces(nodes, x, y, z, m, 0.5, 1.0, 0.1, leaf_cap=1)
+    for a, b in zip(ref, one):
+        np.testing.assert_array_equal(a, b)
+    dx, dy, dz = orc.direct_f64(x, y, z, m, 1.0, 0.1)
+    for cap, theta in ((n, 0.5), (8, 0.0)):
+        bx, by, bz, inter = orc.bh_forces(nodes, x, y, z, m, theta, 1.0, 0.1, leaf_cap=cap)
+        assert (inter == n - 1).all(), (cap, theta)
+        for b, d in ((bx, dx), (by, dy), (bz, dz)):
+            assert rel_err(b, d, 1e-3).max() < 1e-4
+    # buckets sit between the two: fewer accepted cells than the reference walk
+    _, _, _, i1 = orc.bh_forces(nodes, x, y, z, m, 0.8, 1.0, 0.1)
+    _, _, _, i8 = orc.bh_forces(nodes, x, y, z, m, 0.8, 1.0, 0.1, leaf_cap=8)
+    assert (i8 >= i1).all() and (i8 <= n - 1).all()
+
+
 def test_direct_grid32_self_consistency(orc, golden):
     # tests/test_force_calculation.cpp:108-148 builds its expectation from the
     # pair function in ascending j; the oracle's direct sum is that loop.
