@@ -63,7 +63,7 @@ def parse():
                     help="--impl reference: CPU seconds spread over warmup + steps")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--case", choices=["direct", "bh", "bh8", "hash", "precision"], default=None,
+    ap.add_argument("--case", choices=["direct", "bh", "bh8", "bhg", "hash", "precision"], default=None,
                     help="time one plain force evaluation of a single system instead "
                          "(small profiling cases), or run the precision study")
     ap.add_argument("--case-n", type=int, default=262144)
@@ -91,9 +91,10 @@ def precision_arm(args, local) -> dict:
 
 
 def case_arm(args, local):
-    """One system through nbgb_compute_forces: direct / Barnes-Hut (theta 0.5,
-    1 or 8 bodies per leaf) on a Plummer sphere, or the spatial hash on the
-    uniform cube at the serving density; prints ms per evaluation."""
+    """One system through nbgb_compute_forces: direct / Barnes-Hut (theta 0.5;
+    1 or 8 bodies per leaf, or the group walk) on a Plummer sphere, or the
+    spatial hash on the uniform cube at the serving density; prints ms per
+    evaluation."""
     import torch
 
     import nbgb
@@ -108,7 +109,8 @@ def case_arm(args, local):
         calc = nbgb.DirectForceCalculator()
     else:
         s = nbgb.ics.two_plummer(n, seed=2)
-        calc = nbgb.BarnesHutCalculator(0.5, leaf_capacity=8 if args.case == "bh8" else 1)
+        calc = nbgb.BarnesHutCalculator(0.5, leaf_capacity=8 if args.case == "bh8" else 1,
+                                        group_walk=args.case == "bhg")
     calc.setSofteningParameter(EPS)
     st = torch.cuda.current_stream()
     calc.set_stream(st.cuda_stream)

@@ -103,6 +103,15 @@ typedef struct nbgb_params {
  * accelerations kept in FP64 (the full-FP64 reference variant; FP64
  * arithmetic runs at a small fraction of the FP32 rate on GB300). */
 #define NBGB_FLAG_FP64 0x8u
+/* Barnes-Hut group walk: the bodies of each small subtree (at most 32,
+ * consecutive small sibling subtrees merged) share one interaction list; a
+ * cell is accepted for the group when its cube does not touch the group's
+ * bounding box and 4h^2 < theta^2 (d^2 + eps^2), d the distance from the
+ * cell's centre of mass to the box.  Every accepted cell passes the
+ * reference's per-target test for every body of the group, so the force
+ * error is at most that of the reference walk at the same theta; the
+ * interaction sets differ from the reference's.  Needs leaf_capacity 1. */
+#define NBGB_FLAG_GROUP_WALK 0x10u
 
 void nbgb_params_default(nbgb_params* p);
 
@@ -313,6 +322,7 @@ typedef struct nbgb_ensemble_config {
   int32_t direct_config;     /* direct kernel configuration; -1 = autotune */
   int32_t use_graphs;        /* run the batched Barnes-Hut pass as a CUDA graph while the
                                 set of resident Barnes-Hut systems is unchanged */
+  int32_t group_walk;        /* 1 = Barnes-Hut group walk (NBGB_FLAG_GROUP_WALK) */
 } nbgb_ensemble_config;
 
 /* One finished request. */
@@ -391,6 +401,15 @@ nbgb_status nbgb_measure_fp32_peak(double* ffma_tflops, double* ffma2_tflops, do
  * NBGB_ERR_DEVICE_TIMEOUT with the device error bits in *error_bits; the
  * context stays usable.  Nothing faults, traps or hangs. */
 nbgb_status nbgb_selftest_wait_timeout(uint32_t max_iters, uint32_t* error_bits);
+
+/* Test hook for the Barnes-Hut group walk: the number of shared-memory stack
+ * entries (64 .. 512, default 512) a warp uses before it spills the older
+ * half of its traversal stack to a global overflow chunk.  Lowering it
+ * exercises the spill path on small inputs; when more warps spill in one
+ * walk than there are overflow chunks (256), or one warp outgrows its chunk,
+ * the walk reports NBGB_ERR_OVERFLOW ("group walk stack overflow") at the
+ * next synchronization instead of returning forces.  Process-wide. */
+nbgb_status nbgb_selftest_group_walk_stack(int32_t entries);
 
 /* ---------------------------------------------------------------------------
  * Library information.

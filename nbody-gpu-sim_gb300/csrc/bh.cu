@@ -44,6 +44,7 @@
 // memory, broadcast node loads).  With leaf_capacity > 1 a subtree holding
 // at most that many bodies is summed body by body when opened.
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "bh.cuh"
@@ -66,21 +67,28 @@ struct __align__(16) Node {
   int4 info;    // skip (next node outside the subtree), depth << 8 | leaf,
                 // first body, body count
   int4 walk;    // for the walk: skip | leaf << 31 | zero mass << 30, bits of 4 h^2,
-                // first body, body count
+                // first body, body count | has a next sibling << 31
 };
 
 constexpr uint32_t kWalkLeaf = 1u << 31;
 constexpr uint32_t kWalkZero = 1u << 30;
+constexpr uint32_t kWalkNext = 1u << 31;  // in walk.w: the node has a next sibling
 constexpr int64_t kMaxWalkNodes = (int64_t)1 << 30;  // skip indices below the flag bits
 
 // The walk record of a node whose centre of mass is final: skip and flags,
 // and the opening test's size2 = 4 h^2 (force_barnes_hut.cu:222) rounded as
 // the reference rounds it.
-__device__ __forceinline__ int4 walk_record(const int4& in, float h, float mass) {
+__device__ __forceinline__ int4 walk_record(const int4& in, float h, float mass, bool next) {
   uint32_t w = (uint32_t)in.x;
   if (in.y & 1) w |= kWalkLeaf;
   if (mass == 0.0f) w |= kWalkZero;
-  return make_int4((int)w, __float_as_int(__fmul_rn(__fmul_rn(4.0f, h), h)), in.z, in.w);
+  return make_int4((int)w, __float_as_int(__fmul_rn(__fmul_rn(4.0f, h), h)), in.z,
+                   (int)((uint32_t)in.w | (next ? kWalkNext : 0u)));
+}
+
+// A node has a next sibling when its subtree ends before its parent's.
+__device__ __forceinline__ bool has_next_sibling(const Node* nodes, int skip, int par) {
+  return par >= 0 && skip < nodes[par].info.x;
 }
 
 struct BHState {
@@ -111,6 +119,9 @@ struct BHState {
   DevBuf<int32_t> node_parent, node_nchild, node_visit;
   DevBuf<float4> spm;      // bodies in path order
   DevBuf<uint32_t> walk_ctr;  // next warp task of the walk
+  DevBuf<int4> groups;        // group walk: first body, count, segment
+  DevBuf<char> group_ctr;     // group walk: GroupCounters
+  DevBuf<int> group_ovf;      // group walk: stack overflow chunks
   int64_t n = 0;
   int64_t reserve = 0;  // bodies the per-body buffers are sized for (>= n)
   int64_t cap = 0;      // node capacity
@@ -630,8 +641,8 @@ __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ 
       m = t;
     }
     nodes[p].com = make_float4(cx, cy, cz, m);
-    nodes[p].walk = walk_record(ip, nodes[p].geom.w, m);
     int node = parent[p];
+    nodes[p].walk = walk_record(ip, nodes[p].geom.w, m, has_next_sibling(nodes, ip.x, node));
     while (node >= 0) {
       // release: this child's centre of mass is visible to the sibling that
       // arrives last; acquire: the last one sees every sibling's
@@ -654,8 +665,9 @@ __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ 
         r.z = __fdiv_rn(sz, tm);
       }
       __stcg(&nodes[node].com, r);
-      nodes[node].walk = walk_record(in, nodes[node].geom.w, r.w);
-      node = parent[node];
+      const int up = parent[node];
+      nodes[node].walk = walk_record(in, nodes[node].geom.w, r.w, has_next_sibling(nodes, in.x, up));
+      node = up;
     }
   }
 }
@@ -810,12 +822,13 @@ __global__ void __launch_bounds__(256, BUCKET ? 6 : (COUNT ? 7 : 8)) bh_walk_ker
         if (COUNT) ++cnt;
         resume = skip;
       }
-      if (BUCKET && wr.w <= a.leaf_cap) {
+      if (BUCKET && (int)((uint32_t)wr.w & ~kWalkNext) <= a.leaf_cap) {
         // a subtree of at most leaf_cap bodies: the lanes that open it sum
         // its bodies directly (all read the same body: one broadcast load)
         if (open) {
           const int64_t self = k - wr.z;
-          for (int j = 0; j < wr.w; ++j) {
+          const int nb = (int)((uint32_t)wr.w & ~kWalkNext);
+          for (int j = 0; j < nb; ++j) {
             const float4 q = __ldg(&a.spm[wr.z + j]);
             if (j != self) {
               bh_add(q.x, q.y, q.z, q.w, pi.x, pi.y, pi.z, a.eps2, sx, sy, sz);
@@ -860,7 +873,7 @@ size_t bh_state_bytes(const BHState* p) {
          h.hist.bytes() + h.scan_ws.bytes() + h.lcp.bytes() + h.ncnt.bytes() + h.nstart.bytes() +
          h.scalars.bytes() + h.nodes.bytes() +
          h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() + h.spm.bytes() +
-         h.walk_ctr.bytes();
+         h.walk_ctr.bytes() + h.groups.bytes() + h.group_ctr.bytes() + h.group_ovf.bytes();
 }
 
 size_t bh_bytes_estimate(int64_t n) { return (size_t)n * 480 + (64u << 10); }
@@ -999,6 +1012,347 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err) {
   NBGB_LAUNCH_CHECK();
 }
 
+// ---------------------------------------------------------- group walk --
+// Barnes-Hut with a per-group opening test: the bodies of one small subtree
+// (or of consecutive small sibling subtrees, at most 32 bodies) share one
+// interaction list, built by one warp that tests 32 nodes at a time.  A cell
+// is accepted for the whole group when its cube does not touch the group's
+// bounding box and size2 < theta2 (d_min^2 + eps^2), d_min being the distance
+// from the cell's centre of mass to the box: every accepted cell passes the
+// reference's per-target test (force_barnes_hut.cu:218-224) for every body of
+// the group, so each target sees an equal or finer cell set than in the
+// reference walk.  Leaves contribute their bodies.  The list is evaluated by
+// all lanes at once, one target per lane, in packed FP32x2 arithmetic.
+constexpr int kGroupSize = 32;        // bodies per group (one per lane)
+constexpr int kGroupMergeMax = 1024;  // sibling subtrees merge only under parents this small
+constexpr int kGStack = 512;          // per-warp shared stack (nodes to test)
+constexpr int kGRing = 64;            // per-warp ring of pending list entries
+constexpr int kOvfChunk = 8704;       // per-warp stack overflow: 32 x 8 siblings x 34 levels
+constexpr int kOvfChunks = 256;       // overflow chunks per launch
+
+struct GroupCounters {
+  uint32_t ngroups;  // groups emitted by group_kernel
+  uint32_t task;     // next group of the walk
+  uint32_t ovf;      // overflow chunks handed out
+  uint32_t pad;
+};
+
+// Groups: roots with at most kGroupSize bodies; below larger nodes, runs of
+// consecutive children with at most kGroupSize bodies in total (merged only
+// when the parent holds at most kGroupMergeMax bodies: sibling cells of a
+// large sparse node can lie far apart); multi-body leaves larger than a
+// group are split.  Every body belongs to exactly one group, and a group is
+// one contiguous range of path-sorted bodies.
+__global__ void group_kernel(const Node* __restrict__ nodes, const uint32_t* __restrict__ nstart,
+                             int64_t n, int64_t cap, const uint32_t* __restrict__ body,
+                             const int32_t* __restrict__ seg_of, int4* __restrict__ groups,
+                             GroupCounters* __restrict__ gc) {
+  const uint32_t total = nstart[n];
+  if ((int64_t)total > cap) return;
+  auto emit = [&](int f, int c) {
+    const uint32_t g = atomicAdd(&gc->ngroups, 1u);
+    groups[g] = make_int4(f, c, seg_of[body[f]], 0);
+  };
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int4 in = nodes[p].info;  // skip, depth << 8 | leaf, first, count
+    if (in.w <= kGroupSize) {
+      if ((in.y >> 8) == 0) emit(in.z, in.w);  // a segment root
+      continue;
+    }
+    if (in.y & 1) {  // depth-32 leaf holding more bodies than a group
+      for (int f = 0; f < in.w; f += kGroupSize) emit(in.z + f, min(kGroupSize, in.w - f));
+      continue;
+    }
+    const bool merge = in.w <= kGroupMergeMax;
+    int gf = 0, gn = 0;
+    for (int c = (int)p + 1; c < in.x;) {
+      const int4 ci = nodes[c].info;
+      if (ci.w > kGroupSize) {
+        if (gn) emit(gf, gn);
+        gn = 0;
+      } else if (gn && merge && gn + ci.w <= kGroupSize) {
+        gn += ci.w;
+      } else {
+        if (gn) emit(gf, gn);
+        gf = ci.z;
+        gn = ci.w;
+      }
+      c = ci.x;
+    }
+    if (gn) emit(gf, gn);
+  }
+}
+
+struct GroupWalkArgs {
+  const Node* nodes;
+  const float4* spm;
+  const uint32_t* body;
+  const uint32_t* nstart;
+  SegView sv;
+  const int4* groups;
+  const int32_t* seg_root;
+  int64_t n;
+  int64_t cap;
+  float theta2;
+  float eps2;
+  float G;
+  float* ax;
+  float* ay;
+  float* az;
+  int32_t* counts;                  // per-body list lengths without the body itself (or null)
+  unsigned long long* inter_total;  // sum of counts (or null)
+  GroupCounters* gc;
+  int* ovf;                         // kOvfChunks x kOvfChunk stack overflow entries
+  uint32_t* err;
+  int stack_limit;                  // shared stack entries used (64 .. kGStack)
+};
+
+// Floats as unsigned integers with the same order (finite values).
+__device__ __forceinline__ uint32_t ord_of(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float float_of(uint32_t o) {
+  return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+// Adds list entries [base, base + cnt) of the ring (cnt a multiple of 4)
+// to the lane's target, two entries per packed operation.
+template <bool ZERO_EPS>
+__device__ __forceinline__ void group_eval(const float* ex, const float* ey, const float* ez,
+                                           const float* em, int base, int cnt, float4 pi,
+                                           float eps2, f2& ax2, f2& ay2, f2& az2) {
+  const f2 px = f2_make(pi.x, pi.x), py = f2_make(pi.y, pi.y), pz = f2_make(pi.z, pi.z);
+  const f2 e2 = f2_make(eps2, eps2);
+#pragma unroll 1
+  for (int j = 0; j < cnt; j += 4) {
+    const float4 X = *reinterpret_cast<const float4*>(ex + base + j);
+    const float4 Y = *reinterpret_cast<const float4*>(ey + base + j);
+    const float4 Z = *reinterpret_cast<const float4*>(ez + base + j);
+    const float4 M = *reinterpret_cast<const float4*>(em + base + j);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const f2 dx = f2_sub(h ? f2_make(X.z, X.w) : f2_make(X.x, X.y), px);
+      const f2 dy = f2_sub(h ? f2_make(Y.z, Y.w) : f2_make(Y.x, Y.y), py);
+      const f2 dz = f2_sub(h ? f2_make(Z.z, Z.w) : f2_make(Z.x, Z.y), pz);
+      const f2 d2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, e2)));
+      float d2l, d2h;
+      f2_split(d2, d2l, d2h);
+      float rl = rsqrt_approx(d2l), rh = rsqrt_approx(d2h);
+      if (ZERO_EPS) {  // coincident bodies (and the target itself) add nothing
+        rl = d2l > 0.0f ? rl : 0.0f;
+        rh = d2h > 0.0f ? rh : 0.0f;
+      }
+      const f2 r = f2_make(rl, rh);
+      const f2 m = h ? f2_make(M.z, M.w) : f2_make(M.x, M.y);
+      const f2 f = f2_mul(f2_mul(m, r), f2_mul(r, r));
+      ax2 = f2_fma(f, dx, ax2);
+      ay2 = f2_fma(f, dy, ay2);
+      az2 = f2_fma(f, dz, az2);
+    }
+  }
+}
+
+template <bool COUNT, bool ZERO_EPS>
+__global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) {
+  __shared__ int s_stack[8][kGStack];
+  __shared__ __align__(16) float s_ring[8][4][kGRing];
+  const uint32_t total = a.nstart[a.n];
+  if ((int64_t)total > a.cap) return;  // the tree build failed and said so
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
+  int* stk = s_stack[wid];
+  float* ex = s_ring[wid][0];
+  float* ey = s_ring[wid][1];
+  float* ez = s_ring[wid][2];
+  float* em = s_ring[wid][3];
+  const uint32_t ngroups = *(volatile uint32_t*)&a.gc->ngroups;
+  int* ovf = nullptr;  // this warp's overflow chunk, taken on first use
+  while (true) {
+    uint32_t t32 = 0;
+    if (lane == 0) t32 = atomicAdd(&a.gc->task, 1u);
+    const uint32_t t = __shfl_sync(full, t32, 0);
+    if (t >= ngroups) break;
+    const int4 g = a.groups[t];  // first, count, segment
+    const bool valid = lane < g.y;
+    const int k = g.x + (valid ? lane : 0);
+    const float4 pi = a.spm[k];
+    const float lox = float_of(__reduce_min_sync(full, ord_of(pi.x)));
+    const float loy = float_of(__reduce_min_sync(full, ord_of(pi.y)));
+    const float loz = float_of(__reduce_min_sync(full, ord_of(pi.z)));
+    const float hix = float_of(__reduce_max_sync(full, ord_of(pi.x)));
+    const float hiy = float_of(__reduce_max_sync(full, ord_of(pi.y)));
+    const float hiz = float_of(__reduce_max_sync(full, ord_of(pi.z)));
+    f2 ax2 = f2_make(0.f, 0.f), ay2 = ax2, az2 = ax2;
+    uint32_t wr = 0, rd = 0;  // list entries written / evaluated
+    uint32_t selfmask = 0;    // lanes whose own body is in the list
+    int sp = 1, gsp = 0;
+    bool failed = false;
+    if (lane == 0) stk[0] = a.seg_root[g.z];
+    __syncwarp();
+    while (sp > 0 || gsp > 0) {
+      if (sp == 0) {  // refill from the overflow chunk
+        const int m = min(gsp, a.stack_limit / 2);
+        for (int j = lane; j < m; j += 32) stk[j] = ovf[gsp - m + j];
+        gsp -= m;
+        sp = m;
+        __syncwarp();
+      }
+      if (sp > a.stack_limit - 32) {  // a step adds at most 32: spill the oldest half
+        const int half = a.stack_limit / 2;
+        if (!ovf) {
+          uint32_t c32 = 0;
+          if (lane == 0) c32 = atomicAdd(&a.gc->ovf, 1u);
+          const uint32_t c = __shfl_sync(full, c32, 0);
+          if (c < (uint32_t)kOvfChunks) ovf = a.ovf + (size_t)c * kOvfChunk;
+        }
+        if (!ovf || gsp + half > kOvfChunk) {
+          failed = true;
+          break;
+        }
+        for (int j = lane; j < half; j += 32) ovf[gsp + j] = stk[j];
+        __syncwarp();
+        for (int j = lane; j < sp - half; j += 32) stk[j] = stk[half + j];
+        gsp += half;
+        sp -= half;
+        __syncwarp();
+      }
+      const int m = min(sp, 32);
+      sp -= m;
+      const bool have = lane < m;
+      const int node = have ? stk[sp + lane] : 0;
+      __syncwarp();
+      f2 cm_xy = f2_make(0.f, 0.f), cm_zw = cm_xy, g_xy = cm_xy, g_zw = cm_xy;
+      int4 w = make_int4((int)kWalkZero, 0, 0, 0);
+      if (have) {
+        ld_node2(&a.nodes[node], cm_xy, cm_zw, g_xy, g_zw);
+        w = __ldg(&a.nodes[node].walk);
+      }
+      float4 cm, ge;
+      f2_split(cm_xy, cm.x, cm.y);
+      f2_split(cm_zw, cm.z, cm.w);
+      f2_split(g_xy, ge.x, ge.y);
+      f2_split(g_zw, ge.z, ge.w);
+      const uint32_t wx = (uint32_t)w.x;
+      const bool next = have && ((uint32_t)w.w & kWalkNext);
+      const int cnt = (int)((uint32_t)w.w & ~kWalkNext);
+      bool entry = false, open = false, multi = false;
+      if (!(wx & kWalkZero)) {
+        if (wx & kWalkLeaf) {
+          entry = cnt == 1;
+          multi = cnt > 1;
+        } else {
+          const bool overlap = __fsub_rn(ge.x, ge.w) <= hix && __fadd_rn(ge.x, ge.w) >= lox &&
+                               __fsub_rn(ge.y, ge.w) <= hiy && __fadd_rn(ge.y, ge.w) >= loy &&
+                               __fsub_rn(ge.z, ge.w) <= hiz && __fadd_rn(ge.z, ge.w) >= loz;
+          const float dx = fmaxf(fmaxf(__fsub_rn(lox, cm.x), __fsub_rn(cm.x, hix)), 0.0f);
+          const float dy = fmaxf(fmaxf(__fsub_rn(loy, cm.y), __fsub_rn(cm.y, hiy)), 0.0f);
+          const float dz = fmaxf(fmaxf(__fsub_rn(loz, cm.z), __fsub_rn(cm.z, hiz)), 0.0f);
+          const float d2 =
+              __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), a.eps2);
+          entry = !overlap && __int_as_float(w.y) < __fmul_rn(a.theta2, d2);
+          open = !entry;
+        }
+      }
+      // next siblings below first children, so the walk goes depth first
+      const unsigned bs = __ballot_sync(full, next), bo = __ballot_sync(full, open);
+      if (next) stk[sp + __popc(bs & lt)] = (int)(wx & (kWalkZero - 1u));
+      if (open) stk[sp + __popc(bs) + __popc(bo & lt)] = node + 1;
+      sp += __popc(bs) + __popc(bo);
+      const unsigned be = __ballot_sync(full, entry);
+      if (entry) {
+        const int slot = (int)((wr + __popc(be & lt)) & (kGRing - 1));
+        ex[slot] = cm.x;
+        ey[slot] = cm.y;
+        ez[slot] = cm.z;
+        em[slot] = cm.w;
+      }
+      wr += __popc(be);
+      if (COUNT) {
+        const uint32_t rel = (uint32_t)(w.z - g.x);
+        selfmask |= __reduce_or_sync(
+            full, (entry && (wx & kWalkLeaf) && rel < (uint32_t)g.y) ? (1u << rel) : 0u);
+      }
+      __syncwarp();
+      if (wr - rd >= 32) {
+        group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, pi, a.eps2, ax2, ay2,
+                             az2);
+        rd += 32;
+        __syncwarp();
+      }
+      // multi-body (depth-32) leaves: their bodies one by one
+      unsigned bm = __ballot_sync(full, multi);
+      while (bm) {
+        const int src = __ffs(bm) - 1;
+        bm &= bm - 1;
+        const int f = __shfl_sync(full, w.z, src), c = __shfl_sync(full, cnt, src);
+        if (COUNT) {
+          const uint32_t o = (uint32_t)(k - f);
+          selfmask |= __ballot_sync(full, valid && o < (uint32_t)c);
+        }
+        for (int b = 0; b < c; b += 32) {
+          const bool e = b + lane < c;
+          if (e) {
+            const float4 q = a.spm[f + b + lane];
+            const int slot = (int)((wr + lane) & (kGRing - 1));
+            ex[slot] = q.x;
+            ey[slot] = q.y;
+            ez[slot] = q.z;
+            em[slot] = q.w;
+          }
+          wr += (uint32_t)min(32, c - b);
+          __syncwarp();
+          if (wr - rd >= 32) {
+            group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, pi, a.eps2, ax2,
+                                 ay2, az2);
+            rd += 32;
+            __syncwarp();
+          }
+        }
+      }
+    }
+    if (failed) {
+      if (lane == 0) raise_error(a.err, kErrWalkStack);
+      const float nan = __int_as_float(0x7fc00000);
+      ax2 = ay2 = az2 = f2_make(nan, nan);
+    } else {
+      // the rest of the list, padded to a multiple of 4 with massless entries
+      const int left = (int)(wr - rd), padded = (left + 3) & ~3;
+      if (lane >= left && lane < padded) {
+        const int slot = (int)((rd + lane) & (kGRing - 1));
+        ex[slot] = 3.0e18f;
+        ey[slot] = 0.0f;
+        ez[slot] = 0.0f;
+        em[slot] = 0.0f;
+      }
+      __syncwarp();
+      if (padded)
+        group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), padded, pi, a.eps2, ax2,
+                             ay2, az2);
+      __syncwarp();
+    }
+    const int cnt_lane = (int)wr - (int)((selfmask >> lane) & 1u);
+    if (valid) {
+      float sx0, sx1, sy0, sy1, sz0, sz1;
+      f2_split(ax2, sx0, sx1);
+      f2_split(ay2, sy0, sy1);
+      f2_split(az2, sz0, sz1);
+      const int64_t i = a.sv.arena(a.body[k]);
+      a.ax[i] = a.G * (sx0 + sx1);
+      a.ay[i] = a.G * (sy0 + sy1);
+      a.az[i] = a.G * (sz0 + sz1);
+      if (COUNT && a.counts) a.counts[i] = cnt_lane;
+    }
+    if (COUNT && a.inter_total) {
+      unsigned long long c = valid ? (unsigned long long)cnt_lane : 0ull;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(full, c, o);
+      if (lane == 0) atomicAdd(a.inter_total, c);
+    }
+  }
+}
+
 // Resident 256-thread blocks per SM of one walk instantiation.
 template <bool COUNT, bool BUCKET>
 static int walk_occupancy() {
@@ -1010,9 +1364,87 @@ static int walk_occupancy() {
   return occ;
 }
 
+template <bool COUNT, bool ZERO_EPS>
+static int group_walk_occupancy() {
+  static const int occ = [] {
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bh_group_walk_kernel<COUNT, ZERO_EPS>, 256,
+                                                  0);
+    return std::max(b, 1);
+  }();
+  return occ;
+}
+
+template <bool COUNT, bool ZERO_EPS>
+static void launch_group_walk(const GroupWalkArgs& g, int64_t n, cudaStream_t st) {
+  // persistent warps: one resident wave, never more warps than bodies
+  const int64_t blocks = std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(n, 8), (int64_t)num_sms() * group_walk_occupancy<COUNT, ZERO_EPS>()));
+  bh_group_walk_kernel<COUNT, ZERO_EPS><<<(unsigned)blocks, 256, 0, st>>>(g);
+}
+
+// Shared stack entries the group walk uses before spilling to global memory
+// (a test hook: lowering it exercises the spill path on small inputs).
+static std::atomic<int> g_group_stack_limit{kGStack};
+
+void bh_set_group_stack_limit(int entries) { g_group_stack_limit.store(entries); }
+
+static void bh_group_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, float* az,
+                          int32_t* counts, unsigned long long* inter_total, uint32_t* err,
+                          cudaStream_t st) {
+  const int64_t n = h.n;
+  int4* groups = grow(h.groups, (size_t)h.reserve);
+  GroupCounters* gc = reinterpret_cast<GroupCounters*>(grow(h.group_ctr, sizeof(GroupCounters)));
+  int* ovf = grow(h.group_ovf, (size_t)kOvfChunks * kOvfChunk);
+  NBGB_CUDA(cudaMemsetAsync(gc, 0, sizeof(GroupCounters), st));
+  group_kernel<<<grid1d(h.cap), 256, 0, st>>>(h.nodes.ptr, h.nstart.ptr, n, h.cap, h.body,
+                                              h.seg_of.ptr, groups, gc);
+  NBGB_LAUNCH_CHECK();
+  GroupWalkArgs g;
+  g.nodes = h.nodes.ptr;
+  g.spm = h.spm.ptr;
+  g.body = h.body;
+  g.nstart = h.nstart.ptr;
+  g.sv = SegView{h.seg_off_p, h.seg_base_p, h.seg_of.ptr, h.box.ptr};
+  g.groups = groups;
+  g.seg_root = h.seg_root.ptr;
+  g.n = n;
+  g.cap = h.cap;
+  g.theta2 = p.theta * p.theta;
+  g.eps2 = p.softening * p.softening;
+  g.G = p.G;
+  g.ax = ax;
+  g.ay = ay;
+  g.az = az;
+  g.counts = counts;
+  g.inter_total = inter_total;
+  g.gc = gc;
+  g.ovf = ovf;
+  g.err = err;
+  g.stack_limit = g_group_stack_limit.load();
+  const bool count = counts != nullptr || inter_total != nullptr;
+  const bool zero_eps = g.eps2 == 0.0f;
+  if (count) {
+    if (zero_eps)
+      launch_group_walk<true, true>(g, n, st);
+    else
+      launch_group_walk<true, false>(g, n, st);
+  } else {
+    if (zero_eps)
+      launch_group_walk<false, true>(g, n, st);
+    else
+      launch_group_walk<false, false>(g, n, st);
+  }
+  NBGB_LAUNCH_CHECK();
+}
+
 // Forces for every segment: acc written at each segment's arena offset.
 void bh_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, float* az, int32_t* counts,
-             unsigned long long* inter_total, cudaStream_t st) {
+             unsigned long long* inter_total, uint32_t* err, cudaStream_t st) {
+  if (p.group_walk) {
+    bh_group_walk(h, p, ax, ay, az, counts, inter_total, err, st);
+    return;
+  }
   WalkArgs w;
   w.nodes = h.nodes.ptr;
   w.spm = h.spm.ptr;
@@ -1091,9 +1523,10 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
     NBGB_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
     h.cap = (int64_t)hs[0] + (int64_t)hs[0] / 8 + 64;
   }
-  BHWalkParams wp{c->params.G, c->params.softening, c->params.theta, c->params.leaf_capacity};
+  BHWalkParams wp{c->params.G, c->params.softening, c->params.theta, c->params.leaf_capacity,
+                  (c->params.flags & NBGB_FLAG_GROUP_WALK) ? 1 : 0};
   const bool count = (c->params.flags & NBGB_FLAG_COUNT_INTERACTIONS) != 0;
-  bh_walk(h, wp, ax, ay, az, count ? c->counts.ensure((size_t)n) : nullptr, nullptr, st);
+  bh_walk(h, wp, ax, ay, az, count ? c->counts.ensure((size_t)n) : nullptr, nullptr, err, st);
 }
 
 // ------------------------------------------------------------- export --

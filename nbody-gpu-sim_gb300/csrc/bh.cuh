@@ -21,6 +21,8 @@ struct BHWalkParams {
   float softening;
   float theta;
   int leaf_capacity;  // > 1: subtrees of at most this many bodies are summed body by body
+  int group_walk;     // 1: one interaction list per group of <= 32 nearby bodies, cells
+                      // accepted by the group's bounding box (leaf_capacity must be 1)
 };
 
 BHState* bh_state_new();
@@ -44,8 +46,10 @@ void bh_reserve_async(BHState& h);
 void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err);
 // Accelerations of all segments, written at each segment's offset into
 // ax/ay/az.  counts (per arena index) and inter_total (running sum) are
-// optional.
+// optional; err receives device error bits (group walk stack overflow).
 void bh_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, float* az, int32_t* counts,
-             unsigned long long* inter_total, cudaStream_t st);
+             unsigned long long* inter_total, uint32_t* err, cudaStream_t st);
+// Shared-memory stack entries of the group walk before it spills (64 .. 512).
+void bh_set_group_stack_limit(int entries);
 
 }  // namespace nbgb

@@ -61,6 +61,7 @@ enum DeviceErrorBits : uint32_t {
   kErrGridCapacity = 1u << 2,   // spatial hash grid larger than its allocation
   kErrQueueOverflow = 1u << 3,  // ensemble work queue overflow
   kErrBadInput = 1u << 4,       // non-finite bounding box or similar
+  kErrWalkStack = 1u << 5,      // Barnes-Hut group walk: traversal stack overflow
 };
 
 __device__ __forceinline__ void raise_error(uint32_t* word, uint32_t bits) {

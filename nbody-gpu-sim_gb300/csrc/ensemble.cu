@@ -508,8 +508,10 @@ static int64_t run_bh_pass(nbgb_ensemble* e) {
   const int k = e->wev_next % kTimingRing;
   harvest_walk(e, k);
   NBGB_CUDA(cudaEventRecord(e->wev0[k], e->bh_stream));
-  const BHWalkParams wp{e->cfg.G, e->cfg.softening, e->cfg.theta, e->cfg.leaf_capacity};
-  bh_walk(*e->bh, wp, e->ax.ptr, e->ay.ptr, e->az.ptr, nullptr, e->d_bh_inter.ptr, e->bh_stream);
+  const BHWalkParams wp{e->cfg.G, e->cfg.softening, e->cfg.theta, e->cfg.leaf_capacity,
+                        e->cfg.group_walk};
+  bh_walk(*e->bh, wp, e->ax.ptr, e->ay.ptr, e->az.ptr, nullptr, e->d_bh_inter.ptr, e->d_err.ptr,
+          e->bh_stream);
   NBGB_CUDA(cudaEventRecord(e->wev1[k], e->bh_stream));
   e->wev_used[k] = true;
   e->wev_next++;
@@ -817,6 +819,7 @@ void nbgb_ensemble_config_default(nbgb_ensemble_config* c) {
   c->leaf_capacity = 1;  // the reference's tree walk (8 = bodies of small subtrees summed directly)
   c->direct_config = -1;
   c->use_graphs = 1;
+  c->group_walk = 0;
 }
 
 nbgb_status nbgb_ensemble_create(const nbgb_ensemble_config* cfg, nbgb_ensemble** out) {
@@ -831,6 +834,10 @@ nbgb_status nbgb_ensemble_create(const nbgb_ensemble_config* cfg, nbgb_ensemble*
     if (!(c.G > 0.f)) fail(NBGB_ERR_INVALID_ARG, "Validation Error: Gravitational constant must be positive and finite");
     if (c.theta < 0.f || c.theta > 2.f) fail(NBGB_ERR_INVALID_ARG, "Validation Error: Barnes-Hut theta must be between 0 and 2");
     if (c.direct_config >= kNumConfigs) fail(NBGB_ERR_INVALID_ARG, "Validation Error: unknown direct configuration");
+    if (c.leaf_capacity < 1 || c.leaf_capacity > 16)
+      fail(NBGB_ERR_INVALID_ARG, "Validation Error: leaf capacity must be between 1 and 16");
+    if (c.group_walk && c.leaf_capacity != 1)
+      fail(NBGB_ERR_INVALID_ARG, "Validation Error: the group walk needs leaf capacity 1");
     if (c.max_resident < 1 || c.hbm_budget_bytes < (1u << 20))
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: budget or resident cap too small");
     auto e = std::make_unique<nbgb_ensemble>();

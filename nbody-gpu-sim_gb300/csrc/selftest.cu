@@ -6,6 +6,7 @@
 // NBGB_ERR_DEVICE_TIMEOUT).  This entry point exercises exactly that path on
 // demand: one thread waits, through the production mbar_wait(), on an
 // mbarrier nothing ever arrives at, with a caller-chosen iteration limit.
+#include "bh.cuh"
 #include "common.cuh"
 #include "runtime.cuh"
 
@@ -43,5 +44,12 @@ extern "C" nbgb_status nbgb_selftest_wait_timeout(uint32_t max_iters, uint32_t* 
   if (error_bits) *error_bits = h;
   if (h & kErrWaitTimeout)
     return set_error(NBGB_ERR_DEVICE_TIMEOUT, "device wait ran out of iterations (self-test)");
+  return NBGB_OK;
+}
+
+extern "C" nbgb_status nbgb_selftest_group_walk_stack(int32_t entries) {
+  if (entries < 64 || entries > 512)
+    return set_error(NBGB_ERR_INVALID_ARG, "Validation Error: stack entries must be in [64, 512]");
+  bh_set_group_stack_limit(entries);
   return NBGB_OK;
 }

@@ -49,7 +49,7 @@ class EnsembleConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_uint64), ("max_resident", C.c_int32),
                 ("direct_max_n", C.c_int32), ("G", C.c_float), ("softening", C.c_float),
                 ("theta", C.c_float), ("leaf_capacity", C.c_int32), ("direct_config", C.c_int32),
-                ("use_graphs", C.c_int32)]
+                ("use_graphs", C.c_int32), ("group_walk", C.c_int32)]
 
 
 class EnsembleResult(C.Structure):
@@ -75,6 +75,7 @@ FLAG_SYNC = 0x1
 FLAG_COMPENSATED = 0x2
 FLAG_COUNT_INTERACTIONS = 0x4
 FLAG_FP64 = 0x8
+FLAG_GROUP_WALK = 0x10
 
 _vp = C.c_void_p
 _i32p = C.POINTER(C.c_int32)
@@ -106,6 +107,7 @@ _SIGS = {
     "nbgb_particles_copy_to_host": (C.c_int, [_pd, _pd]),
     "nbgb_init_params_default": (None, [C.POINTER(InitParams), C.c_int32]),
     "nbgb_selftest_wait_timeout": (C.c_int, [C.c_uint32, C.POINTER(C.c_uint32)]),
+    "nbgb_selftest_group_walk_stack": (C.c_int, [C.c_int32]),
     "nbgb_init_particles_device": (C.c_int, [_pd, C.POINTER(InitParams), C.c_uint64, _vp]),
     "nbgb_bh_tree_stats": (C.c_int, [_vp, _i32p, _i32p]),
     "nbgb_bh_copy_sorted_keys": (C.c_int, [_vp, _vp, _vp, C.c_size_t]),

@@ -14,8 +14,8 @@ from enum import IntEnum
 import numpy as np
 
 from . import _lib
-from ._lib import (FLAG_COMPENSATED, FLAG_COUNT_INTERACTIONS, FLAG_FP64, FLAG_SYNC, OctreeNode,
-                   Params)
+from ._lib import (FLAG_COMPENSATED, FLAG_COUNT_INTERACTIONS, FLAG_FP64, FLAG_GROUP_WALK,
+                   FLAG_SYNC, OctreeNode, Params)
 from ._lib import ParticleDataStruct
 
 FIELDS = ("pos_x", "pos_y", "pos_z", "vel_x", "vel_y", "vel_z", "acc_x", "acc_y", "acc_z",
@@ -287,10 +287,12 @@ class BarnesHutCalculator(ForceCalculator):
     method = ForceMethod.BARNES_HUT
 
     def __init__(self, theta: float = 0.5, leaf_capacity: int = 1,
-                 params: Params | None = None) -> None:
+                 params: Params | None = None, group_walk: bool = False) -> None:
         p = params if params is not None else default_params()
         p.theta = theta
         p.leaf_capacity = leaf_capacity
+        if group_walk:
+            p.flags |= FLAG_GROUP_WALK
         super().__init__(p)
 
     def setTheta(self, theta: float) -> None:  # noqa: N802
@@ -470,5 +472,6 @@ __all__ = ["ForceMethod", "forceMethodToString", "ParticleData", "ParticleDataMa
            "BarnesHutCalculator", "SpatialHashCalculator", "createForceCalculator",
            "Integrator", "System", "ValidationException", "ResourceException", "CudaException",
            "DeviceTimeout", "CapacityError", "NbodyError", "check", "default_params",
-           "FLAG_SYNC", "FLAG_COMPENSATED", "FLAG_COUNT_INTERACTIONS", "FLAG_FP64", "OctreeNode",
+           "FLAG_SYNC", "FLAG_COMPENSATED", "FLAG_COUNT_INTERACTIONS", "FLAG_FP64", "FLAG_GROUP_WALK",
+           "OctreeNode",
            "Params"]

@@ -590,6 +590,166 @@ int orc_bh_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* 
   return bad ? ORC_ERR_ARG : ORC_OK;
 }
 
+/* Group walk (the library's NBGB_FLAG_GROUP_WALK; the reference has no
+ * such walk -- it restates the same tree and opening quantities, see
+ * orc_bh_forces above).  Groups: the root if it holds at most 32 bodies;
+ * below a larger node, runs of consecutive children (octant order) holding
+ * at most 32 bodies in total, merged only when the parent holds at most 1024
+ * bodies; a child of more than 32 bodies ends the run.  Each group walks the
+ * tree once from the root: a node of zero mass is skipped, a leaf adds its
+ * body, an internal node is accepted (its centre of mass added) when its
+ * cube does not touch the group's bounding box (closed intervals, c -+ h
+ * rounded) and 4h^2 < theta^2 * (fma(dz,dz, fma(dy,dy, dx*dx)) + eps^2),
+ * d the per-axis distance of the centre of mass outside the box, else its
+ * children are walked.  Every body of the group sums the whole list;
+ * interactions per body = list length minus its own leaf.  With eps = 0 a
+ * zero-distance entry adds nothing.  Multi-body (depth-32) leaves are not
+ * supported here (their bodies are not listed in the node records):
+ * returns ORC_ERR_ARG. */
+#define ORC_GROUP 32
+#define ORC_GROUP_MERGE 1024
+
+typedef struct {
+  int nmem;
+  int mem[8];
+} orc_group;
+
+static void orc_group_bodies(const orc_node* nodes, int ni, int* out, int* nb, int* bad) {
+  const orc_node* nd = &nodes[ni];
+  if (nd->is_leaf) {
+    if (nd->particle_count != 1 || *nb >= ORC_GROUP) {
+      *bad = 1;
+      return;
+    }
+    out[(*nb)++] = nd->particle_index;
+    return;
+  }
+  for (int c = 0; c < 8; c++)
+    if (nd->children[c] >= 0) orc_group_bodies(nodes, nd->children[c], out, nb, bad);
+}
+
+int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* x,
+                        const float* y, const float* z, const float* m, float theta, float G,
+                        float eps, float* ax, float* ay, float* az, int32_t* interactions) {
+  if (num_nodes < 1) return ORC_ERR_ARG;
+  /* groups, by a pre-order pass over the nodes of more than ORC_GROUP bodies */
+  orc_group* groups = (orc_group*)malloc(sizeof(orc_group) * (size_t)(n + 1));
+  int* st = (int*)malloc(sizeof(int) * (size_t)(num_nodes + 8));
+  int64_t ng = 0;
+  int bad = 0, sp = 0;
+  if (nodes[0].particle_count <= ORC_GROUP) {
+    groups[ng].nmem = 1;
+    groups[ng++].mem[0] = 0;
+  } else {
+    st[sp++] = 0;
+  }
+  while (sp > 0) {
+    const orc_node* nd = &nodes[st[--sp]];
+    if (nd->is_leaf) {
+      bad = 1; /* a leaf of more than ORC_GROUP bodies */
+      continue;
+    }
+    int merge = nd->particle_count <= ORC_GROUP_MERGE, gn = 0;
+    for (int c = 0; c < 8; c++) {
+      int ch = nd->children[c];
+      if (ch < 0) continue;
+      int cc = nodes[ch].particle_count;
+      if (cc > ORC_GROUP) {
+        gn = 0;
+        st[sp++] = ch;
+      } else if (gn && merge && gn + cc <= ORC_GROUP) {
+        groups[ng - 1].mem[groups[ng - 1].nmem++] = ch;
+        gn += cc;
+      } else {
+        groups[ng].nmem = 1;
+        groups[ng++].mem[0] = ch;
+        gn = cc;
+      }
+    }
+  }
+  free(st);
+  float theta2 = theta * theta, eps2 = eps * eps;
+#pragma omp parallel for schedule(dynamic, 16) reduction(| : bad)
+  for (int64_t g = 0; g < ng; g++) {
+    int body[ORC_GROUP], nb = 0, gbad = 0;
+    for (int j = 0; j < groups[g].nmem; j++) orc_group_bodies(nodes, groups[g].mem[j], body, &nb, &gbad);
+    if (gbad) {
+      bad = 1;
+      continue;
+    }
+    float lo[3] = {x[body[0]], y[body[0]], z[body[0]]}, hi[3] = {lo[0], lo[1], lo[2]};
+    for (int j = 1; j < nb; j++) {
+      const float p[3] = {x[body[j]], y[body[j]], z[body[j]]};
+      for (int a = 0; a < 3; a++) {
+        if (p[a] < lo[a]) lo[a] = p[a];
+        if (p[a] > hi[a]) hi[a] = p[a];
+      }
+    }
+    /* interaction list */
+    int cap = 4096, len = 0, own[ORC_GROUP] = {0};
+    float* list = (float*)malloc(sizeof(float) * 4 * (size_t)cap);
+    int* stk = (int*)malloc(sizeof(int) * (size_t)(num_nodes + 8));
+    int s = 0;
+    stk[s++] = 0;
+    while (s > 0) {
+      const orc_node* nd = &nodes[stk[--s]];
+      if (nd->mass == 0.0f) continue;
+      int entry = 0;
+      if (nd->is_leaf) {
+        entry = 1;
+        for (int j = 0; j < nb; j++)
+          if (body[j] == nd->particle_index) own[j] = 1;
+      } else {
+        int overlap = nd->cx - nd->half <= hi[0] && nd->cx + nd->half >= lo[0] &&
+                      nd->cy - nd->half <= hi[1] && nd->cy + nd->half >= lo[1] &&
+                      nd->cz - nd->half <= hi[2] && nd->cz + nd->half >= lo[2];
+        float dx = fmaxf(fmaxf(lo[0] - nd->comx, nd->comx - hi[0]), 0.0f);
+        float dy = fmaxf(fmaxf(lo[1] - nd->comy, nd->comy - hi[1]), 0.0f);
+        float dz = fmaxf(fmaxf(lo[2] - nd->comz, nd->comz - hi[2]), 0.0f);
+        float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) + eps2;
+        float size2 = 4.0f * nd->half * nd->half;
+        entry = !overlap && size2 < theta2 * d2;
+        if (!entry)
+          for (int c = 7; c >= 0; c--)
+            if (nd->children[c] >= 0) stk[s++] = nd->children[c];
+      }
+      if (entry) {
+        if (len == cap) {
+          cap *= 2;
+          list = (float*)realloc(list, sizeof(float) * 4 * (size_t)cap);
+        }
+        list[4 * len] = nd->comx;
+        list[4 * len + 1] = nd->comy;
+        list[4 * len + 2] = nd->comz;
+        list[4 * len + 3] = nd->mass;
+        len++;
+      }
+    }
+    for (int j = 0; j < nb; j++) {
+      int i = body[j];
+      float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+      for (int e = 0; e < len; e++) {
+        float ex = list[4 * e] - x[i], ey = list[4 * e + 1] - y[i], ez = list[4 * e + 2] - z[i];
+        float e2 = fmaf(ez, ez, fmaf(ey, ey, ex * ex)) + eps2;
+        if (e2 == 0.0f) continue;
+        float inv = 1.0f / sqrtf(e2);
+        float f = list[4 * e + 3] * (inv * inv * inv);
+        sx += f * ex;
+        sy += f * ey;
+        sz += f * ez;
+      }
+      ax[i] = G * sx;
+      ay[i] = G * sy;
+      az[i] = G * sz;
+      if (interactions) interactions[i] = len - own[j];
+    }
+    free(list);
+    free(stk);
+  }
+  free(groups);
+  return bad ? ORC_ERR_ARG : ORC_OK;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Spatial hash                                                             */
 /* ------------------------------------------------------------------------ */

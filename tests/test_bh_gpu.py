@@ -22,12 +22,13 @@ from treeutil import compare
 pytestmark = pytest.mark.gpu
 
 
-def _bh(nb, s, theta=0.5, eps=0.01, leaf=1, count=True, G=1.0):
-    calc = nb.BarnesHutCalculator(theta, leaf_capacity=leaf)
+def _bh(nb, s, theta=0.5, eps=0.01, leaf=1, count=True, G=1.0, group=False):
+    calc = nb.BarnesHutCalculator(theta, leaf_capacity=leaf, group_walk=group)
     calc.setGravitationalConstant(G)
     calc.setSofteningParameter(eps)
     if count:
-        calc.set_flags(nb.FLAG_SYNC | nb.FLAG_COUNT_INTERACTIONS | nb.FLAG_COMPENSATED)
+        calc.set_flags(nb.FLAG_SYNC | nb.FLAG_COUNT_INTERACTIONS | nb.FLAG_COMPENSATED |
+                       (nb.FLAG_GROUP_WALK if group else 0))
     n = len(s["x"])
     with nb.ScopedParticleData(n, {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"],
                                    "mass": s["m"]}) as p:
@@ -148,6 +149,92 @@ def test_bucket_interaction_sets_match_oracle_walk(nb, orc, gen, n, theta, leaf)
     assert np.percentile(err, 99) <= 1e-5, np.percentile(err, 99)
 
 
+def _gen(nb, gen, n):
+    return {"plummer": lambda: nb.ics.plummer(n, seed=n),
+            "two": lambda: nb.ics.two_plummer(n, seed=3),
+            "cube": lambda: nb.ics.uniform_cube(n, seed=4),
+            "far": lambda: nb.ics.plummer(n, seed=11, center=(2000.0, -1500.0, 700.0)),
+            "dense": lambda: nb.ics.plummer(n, seed=12, a=0.01)}[gen]()
+
+
+@pytest.mark.parametrize("gen,n,theta,eps", [("plummer", 5000, 0.5, 0.01), ("plummer", 20000, 0.3, 0.01),
+                                             ("two", 50000, 0.5, 0.01), ("cube", 30000, 0.5, 0.01),
+                                             ("far", 6000, 0.5, 0.01), ("dense", 6000, 0.5, 0.01),
+                                             ("plummer", 3000, 1.0, 0.01), ("plummer", 4000, 0.5, 0.0)])
+def test_group_walk_matches_oracle(nb, orc, gen, n, theta, eps):
+    """Group walk: per-body list lengths (interactions) equal the oracle's
+    group walk on the same tree -- same groups, same bounding boxes, same
+    acceptance arithmetic -- and forces agree within 1e-5 (p99, vector
+    relative; the list order differs).  eps = 0 runs the zero-softening
+    variant (zero-distance entries add nothing)."""
+    s = _gen(nb, gen, n)
+    _, _, nodes, _, merges = _oracle_tree(orc, s)
+    assert merges == 0
+    r = _bh(nb, s, theta=theta, eps=eps, group=True)
+    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], theta, 1.0, eps)
+    np.testing.assert_array_equal(r["inter"], oint)
+    err = vec_rel_err(*r["acc"], ox, oy, oz)
+    assert np.percentile(err, 99) <= 1e-5, np.percentile(err, 99)
+
+
+def test_group_walk_theta0_is_direct_sum(nb, orc):
+    n = 3000
+    s = nb.ics.plummer(n, seed=21)
+    r = _bh(nb, s, theta=0.0, group=True)
+    assert (r["inter"] == n - 1).all()
+    bx, by, bz = orc.direct_f64(s["x"], s["y"], s["z"], s["m"], 1.0, 0.01)
+    assert np.max(vec_rel_err(*r["acc"], bx, by, bz)) < 1e-4
+
+
+def test_group_walk_is_more_accurate_than_reference_walk(nb, orc):
+    # every accepted cell passes the per-target test for each body of the group
+    n = 65536
+    s = nb.ics.two_plummer(n, seed=8)
+    t = np.random.default_rng(9).choice(n, 2048, replace=False)
+    bx, by, bz = orc.direct_f64(s["x"], s["y"], s["z"], s["m"], 1.0, 0.01, targets=t)
+    e1 = vec_rel_err(*(a[t] for a in _bh(nb, s, count=False)["acc"]), bx, by, bz)
+    eg = vec_rel_err(*(a[t] for a in _bh(nb, s, count=False, group=True)["acc"]), bx, by, bz)
+    assert np.median(eg) < np.median(e1) and np.median(eg) <= 1e-3, (np.median(eg), np.median(e1))
+
+
+@pytest.fixture
+def small_group_stack(nb):
+    from nbgb import _lib
+    nb.check(_lib.lib().nbgb_selftest_group_walk_stack(64))
+    yield
+    nb.check(_lib.lib().nbgb_selftest_group_walk_stack(512))
+
+
+def test_group_walk_spill_path(nb, orc, small_group_stack):
+    """With a 64-entry shared stack every group spills to its global overflow
+    chunk and reloads: the same lists as the oracle's."""
+    n = 1500
+    s = nb.ics.plummer(n, seed=22)
+    _, _, nodes, _, _ = _oracle_tree(orc, s)
+    r = _bh(nb, s, theta=0.2, group=True)
+    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.2, 1.0, 0.01)
+    np.testing.assert_array_equal(r["inter"], oint)
+    assert np.percentile(vec_rel_err(*r["acc"], ox, oy, oz), 99) <= 1e-5
+
+
+def test_group_walk_overflow_is_reported(nb, small_group_stack):
+    """More spilling warps than overflow chunks: the walk reports an overflow
+    status (no fault), and the next call with the normal stack succeeds."""
+    from nbgb import _lib
+    n = 20000
+    s = nb.ics.plummer(n, seed=23)
+    with pytest.raises(nb.NbodyError, match="group walk stack overflow"):
+        _bh(nb, s, theta=0.0, group=True)
+    nb.check(_lib.lib().nbgb_selftest_group_walk_stack(512))
+    r = _bh(nb, s, theta=0.5, group=True)
+    assert np.isfinite(r["acc"][0]).all()
+
+
+def test_group_walk_rejects_buckets(nb):
+    with pytest.raises(nb.ValidationException):
+        nb.BarnesHutCalculator(0.5, leaf_capacity=8, group_walk=True)
+
+
 def test_small_theta_matches_direct(nb, golden):
     # tests/test_spatial_hash.cpp:171-228: theta = 0.1 vs direct < 2 % per
     # component (the canonical tree; the reference's 2N budget merge would
@@ -246,7 +333,8 @@ def test_full_size_two_plummer(nb, orc):
     np.testing.assert_array_equal(r8["inter"][t], oint)
     err8 = vec_rel_err(*(a[t] for a in r8["acc"]), bx, by, bz)
     assert np.median(err8) <= 2e-3
-    r8 = _bh(nb, s, theta=0.5, leaf=8, count=False)
-    err8 = vec_rel_err(*(a[t] for a in r8["acc"]), bx, by, bz)
-    assert np.median(err8) <= 2e-3
+    # and with the group walk: lower error than the reference walk
+    rg = _bh(nb, s, theta=0.5, count=False, group=True)
+    errg = vec_rel_err(*(a[t] for a in rg["acc"]), bx, by, bz)
+    assert np.median(errg) <= np.median(err)
 

@@ -153,14 +153,15 @@ def test_autotuner_settles(nb):
     ens.close()
 
 
-def test_batched_bh_bitwise_vs_calculator(nb):
+@pytest.mark.parametrize("group_walk", [0, 1])
+def test_batched_bh_bitwise_vs_calculator(nb, group_walk):
     """Barnes-Hut systems of uneven N (one body, two bodies, ragged tails of
     the 32-target warp tasks, two clusters) share one batched build + walk;
     each system's final acceleration equals the single-system calculator's
-    on the same FP32 positions bit for bit."""
+    on the same FP32 positions bit for bit (reference walk and group walk)."""
     from nbgb.serving import Ensemble
     sizes = (1, 2, 33, 1500, 4097, 12000)
-    ens = Ensemble(direct_max_n=0, hbm_budget_bytes=2 << 30)
+    ens = Ensemble(direct_max_n=0, hbm_budget_bytes=2 << 30, group_walk=group_walk)
     reqs = {}
     for i, n in enumerate(sizes):
         s = nb.ics.plummer(n, seed=70 + i) if n != 4097 else nb.ics.two_plummer(n, seed=70 + i)
@@ -179,13 +180,13 @@ def test_batched_bh_bitwise_vs_calculator(nb):
     assert st["bh_walk_ms"] > 0
     for rid, s in got.items():
         pos = {k: s[k].astype(np.float32) for k in ("x", "y", "z")}
-        ref = _calc_bh(nb, pos, s["m"])
+        ref = _calc_bh(nb, pos, s["m"], group_walk=group_walk)
         for k, a in zip(("ax", "ay", "az"), ref):
             np.testing.assert_array_equal(s[k], a, err_msg=f"n={reqs[rid]} {k}")
 
 
-def _calc_bh(nb, pos, m, theta=0.5, eps=0.01):
-    calc = nb.BarnesHutCalculator(theta)
+def _calc_bh(nb, pos, m, theta=0.5, eps=0.01, group_walk=0):
+    calc = nb.BarnesHutCalculator(theta, group_walk=bool(group_walk))
     calc.setSofteningParameter(eps)
     n = len(m)
     with nb.ScopedParticleData(n, {"pos_x": pos["x"], "pos_y": pos["y"], "pos_z": pos["z"],
@@ -197,13 +198,15 @@ def _calc_bh(nb, pos, m, theta=0.5, eps=0.01):
     return acc
 
 
-def test_batched_bh_many_segments_degenerate(nb):
+@pytest.mark.parametrize("group_walk", [0, 1])
+def test_batched_bh_many_segments_degenerate(nb, group_walk):
     """300 Barnes-Hut systems in one batched pass (a two-digit segment sort),
     among them coincident bodies (depth-32 leaves), zero-mass bodies (skipped
     subtrees) and single bodies: each equals the single-system calculator
     bit for bit."""
     from nbgb.serving import Ensemble
-    ens = Ensemble(direct_max_n=0, max_resident=400, hbm_budget_bytes=2 << 30)
+    ens = Ensemble(direct_max_n=0, max_resident=400, hbm_budget_bytes=2 << 30,
+                   group_walk=group_walk)
     reqs = {}
     for i in range(300):
         n = 1 + (i * 7) % 40
@@ -225,6 +228,6 @@ def test_batched_bh_many_segments_degenerate(nb):
     assert len(got) == len(reqs)
     for rid, s in got.items():
         pos = {k: s[k].astype(np.float32) for k in ("x", "y", "z")}
-        ref = _calc_bh(nb, pos, s["m"])
+        ref = _calc_bh(nb, pos, s["m"], group_walk=group_walk)
         for k, a in zip(("ax", "ay", "az"), ref):
             np.testing.assert_array_equal(s[k], a, err_msg=f"request {rid} n={reqs[rid]} {k}")
