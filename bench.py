@@ -40,8 +40,8 @@ import numpy as np  # noqa: E402
 METRIC = "batched vs plain particle-steps/s on 1 GB300 at stated force err; p99 latency"
 UNIT = "particle-steps/s"
 WORKLOAD = ("ensemble serving: Plummer clusters (a=1, M=1), N log-uniform [256, 65536], "
-            "steps U[100, 2000], eps=0.01, dt=1e-3, direct N<=8192 else Barnes-Hut theta=0.5, "
-            "FP32 forces + FP64 state, 64 GiB admission budget")
+            "steps U[100, 2000], eps=0.01, dt=1e-3, direct N<=8192 else Barnes-Hut theta=0.5 "
+            "(group walk), FP32 forces + FP64 state, 64 GiB admission budget")
 DT = 1e-3
 EPS = 0.01
 L2_BYTES = 129 * 1024 * 1024
@@ -313,9 +313,9 @@ def gpu_arm(args, rank, world, local):
         w_achieved = 20.0 * bh_int / (walk_ms / 1e3) / 1e12 if walk_ms > 0 else None
         walk_share = (walk_ms / 1e3) / elapsed_s if elapsed_s > 0 else None
         direct_share = (dms / 1e3) / elapsed_s if elapsed_s > 0 else None
-        # DRAM bytes of one walk launch: ncu capture at N = 1,048,576 (two
-        # Plummer spheres, 147.6 MB read + written), scaled by the bodies walked
-        walk_traffic = 147.6e6 * bh_bodies / 1048576 if bh_bodies else None
+        # DRAM bytes of one group-walk launch: ncu capture at N = 1,048,576
+        # (two Plummer spheres, 215.6 MB read + written), scaled by the bodies
+        walk_traffic = 215.6e6 * bh_bodies / 1048576 if bh_bodies else None
         clocks = clk.summary()
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -330,9 +330,12 @@ def gpu_arm(args, rank, world, local):
                       f"L2 {L2_BYTES / 2**20:.0f} MiB",
                 "direct_kernel_config": tuned, "theta": 0.5, "softening": EPS, "dt": DT,
                 "force_error": "direct: compensated FP32, median rel err ~1e-7 vs FP64; "
-                               "Barnes-Hut theta=0.5: median rel err <= 2e-3 vs FP64 "
-                               "(tests/test_bh_gpu.py, tests/test_direct_gpu.py); measured "
-                               "on served systems: force_error_measured",
+                               "Barnes-Hut theta=0.5 group walk (each accepted cell passes "
+                               "the reference's per-target test for every body of its "
+                               "group): median rel err <= 1e-3 vs FP64, below the reference "
+                               "walk's (tests/test_bh_gpu.py, tests/test_direct_gpu.py); "
+                               "measured on served systems: force_error_measured",
+                "bh_walk": "group walk (NBGB_FLAG_GROUP_WALK); the plain runs use the same",
                 "parallelism": f"replicas x{world} (request-stream shards)",
             },
             "force_error_measured": force_err,
@@ -354,19 +357,22 @@ def gpu_arm(args, rank, world, local):
                              "API: host arrays submitted, results polled to the host"}
                     if serve_rep else None),
             "roofline": {
-                "kernel": "bh_walk_kernel (batched Barnes-Hut walk, all resident BH systems)",
+                "kernel": "bh_group_walk_kernel (batched Barnes-Hut group walk, all resident "
+                          "BH systems)",
                 "bound": "fp32", "achieved": w_achieved, "peak": ffma_peak, "unit": "TFLOP/s",
                 "frac": (w_achieved / ffma_peak) if w_achieved else None,
                 "traffic": walk_traffic,
                 "traffic_source": "ncu dram__bytes_read+write of one walk at N=1,048,576 "
-                                  "(profiles/bh_walk_two_plummer_1M.md), scaled by bodies walked",
+                                  "(profiles/bh_group_walk_two_plummer_1M.md), scaled by "
+                                  "bodies walked",
                 "algorithmic_bytes": 64 * 1.5 * bh_bodies + 28 * bh_bodies if bh_bodies else None,
                 "peak_source": "measured in-process: FFMA chains on every SM "
                                "(nbgb_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                 "flops_per_interaction": 20, "share_of_tick": walk_share,
                 "walk_ms_per_tick": walk_ms / args.steps,
-                "note": "issue-bound tree walk: ~78 thread instructions per accepted "
-                        "interaction, 83 % issue-active (ncu)",
+                "note": "list evaluation in packed FP32x2 dominates: FMA pipe 61 % and "
+                        "issue 71 % active (ncu, N=1M); interactions counted per lane "
+                        "(list length minus the body itself)",
                 "hbm_peak_gbs_measured": measured_peaks().get("hbm_gbs"),
             },
             "direct_kernel": {"kernel": "ens_direct_kernel (direct-sum work queue)",
@@ -432,10 +438,11 @@ def plain_arm(nbgb, reqs, steps) -> dict:
         s = make_state(nbgb, r)
         if r["n"] <= 8192:
             calc = nbgb.DirectForceCalculator()
-        else:
-            calc = nbgb.BarnesHutCalculator(0.5)
+        else:  # the serving engine's walk, so both runs have the same accuracy
+            calc = nbgb.BarnesHutCalculator(0.5, group_walk=True)
         calc.setSofteningParameter(EPS)
-        calc.set_flags(nbgb.FLAG_COMPENSATED)  # asynchronous: no per-step read-back
+        # asynchronous: no per-step read-back
+        calc.set_flags(calc.params.flags & ~nbgb.FLAG_SYNC)
         sysm = nbgb.System(calc, s)
         sysm.step(DT, 2)  # warm
         calc.synchronize()

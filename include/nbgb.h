@@ -322,7 +322,8 @@ typedef struct nbgb_ensemble_config {
   int32_t direct_config;     /* direct kernel configuration; -1 = autotune */
   int32_t use_graphs;        /* run the batched Barnes-Hut pass as a CUDA graph while the
                                 set of resident Barnes-Hut systems is unchanged */
-  int32_t group_walk;        /* 1 = Barnes-Hut group walk (NBGB_FLAG_GROUP_WALK) */
+  int32_t group_walk;        /* 1 (default) = Barnes-Hut group walk (NBGB_FLAG_GROUP_WALK);
+                                0 = the reference's per-target walk (leaf_capacity applies) */
 } nbgb_ensemble_config;
 
 /* One finished request. */
