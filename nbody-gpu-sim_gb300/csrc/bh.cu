@@ -1118,15 +1118,16 @@ __device__ __forceinline__ float float_of(uint32_t o) {
 }
 
 // Adds list entries [base, base + cnt) of the ring (cnt a multiple of 4)
-// to the lane's target, two entries per packed operation.
+// to the lane's target, two entries per packed operation.  With rep > 1
+// lanes of a small group, replica r of a body takes every rep-th quad.
 template <bool ZERO_EPS>
 __device__ __forceinline__ void group_eval(const float* ex, const float* ey, const float* ez,
-                                           const float* em, int base, int cnt, float4 pi,
-                                           float eps2, f2& ax2, f2& ay2, f2& az2) {
+                                           const float* em, int base, int cnt, int r, int rep,
+                                           float4 pi, float eps2, f2& ax2, f2& ay2, f2& az2) {
   const f2 px = f2_make(pi.x, pi.x), py = f2_make(pi.y, pi.y), pz = f2_make(pi.z, pi.z);
   const f2 e2 = f2_make(eps2, eps2);
 #pragma unroll 1
-  for (int j = 0; j < cnt; j += 4) {
+  for (int j = 4 * r; j < cnt; j += 4 * rep) {
     const float4 X = *reinterpret_cast<const float4*>(ex + base + j);
     const float4 Y = *reinterpret_cast<const float4*>(ey + base + j);
     const float4 Z = *reinterpret_cast<const float4*>(ez + base + j);
@@ -1158,6 +1159,7 @@ template <bool COUNT, bool ZERO_EPS>
 __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) {
   __shared__ int s_stack[8][kGStack];
   __shared__ __align__(16) float s_ring[8][4][kGRing];
+  __shared__ __align__(16) float4 s_box[8][2];  // group bounds: lo, hi
   const uint32_t total = a.nstart[a.n];
   if ((int64_t)total > a.cap) return;  // the tree build failed and said so
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1175,18 +1177,28 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
     const uint32_t t = __shfl_sync(full, t32, 0);
     if (t >= ngroups) break;
     const int4 g = a.groups[t];  // first, count, segment
-    const bool valid = lane < g.y;
-    const int k = g.x + (valid ? lane : 0);
+    // a group of at most 8 (16) bodies gives each body 4 (2) lanes, each
+    // summing a share of the list: lane = replica * gw + body
+    const int gw = g.y <= 8 ? 8 : (g.y <= 16 ? 16 : 32);
+    const int rep = 32 / gw, tl = lane & (gw - 1), rr = lane / gw;
+    const bool valid = tl < g.y;
+    const int k = g.x + (valid ? tl : 0);
     const float4 pi = a.spm[k];
-    const float lox = float_of(__reduce_min_sync(full, ord_of(pi.x)));
-    const float loy = float_of(__reduce_min_sync(full, ord_of(pi.y)));
-    const float loz = float_of(__reduce_min_sync(full, ord_of(pi.z)));
-    const float hix = float_of(__reduce_max_sync(full, ord_of(pi.x)));
-    const float hiy = float_of(__reduce_max_sync(full, ord_of(pi.y)));
-    const float hiz = float_of(__reduce_max_sync(full, ord_of(pi.z)));
+    {
+      const float lox = float_of(__reduce_min_sync(full, ord_of(pi.x)));
+      const float loy = float_of(__reduce_min_sync(full, ord_of(pi.y)));
+      const float loz = float_of(__reduce_min_sync(full, ord_of(pi.z)));
+      const float hix = float_of(__reduce_max_sync(full, ord_of(pi.x)));
+      const float hiy = float_of(__reduce_max_sync(full, ord_of(pi.y)));
+      const float hiz = float_of(__reduce_max_sync(full, ord_of(pi.z)));
+      if (lane == 0) {
+        s_box[wid][0] = make_float4(lox, loy, loz, 0.f);
+        s_box[wid][1] = make_float4(hix, hiy, hiz, 0.f);
+      }
+    }
     f2 ax2 = f2_make(0.f, 0.f), ay2 = ax2, az2 = ax2;
     uint32_t wr = 0, rd = 0;  // list entries written / evaluated
-    uint32_t selfmask = 0;    // lanes whose own body is in the list
+    uint32_t selfmask = 0;    // bodies (by index in the group) whose own leaf is in the list
     int sp = 1, gsp = 0;
     bool failed = false;
     if (lane == 0) stk[0] = a.seg_root[g.z];
@@ -1243,6 +1255,8 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
           entry = cnt == 1;
           multi = cnt > 1;
         } else {
+          const float4 lo = s_box[wid][0], hi = s_box[wid][1];
+          const float lox = lo.x, loy = lo.y, loz = lo.z, hix = hi.x, hiy = hi.y, hiz = hi.z;
           const bool overlap = __fsub_rn(ge.x, ge.w) <= hix && __fadd_rn(ge.x, ge.w) >= lox &&
                                __fsub_rn(ge.y, ge.w) <= hiy && __fadd_rn(ge.y, ge.w) >= loy &&
                                __fsub_rn(ge.z, ge.w) <= hiz && __fadd_rn(ge.z, ge.w) >= loz;
@@ -1269,15 +1283,14 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
         em[slot] = cm.w;
       }
       wr += __popc(be);
-      if (COUNT) {
+      if (COUNT) {  // lane-local here, combined over the warp at the end
         const uint32_t rel = (uint32_t)(w.z - g.x);
-        selfmask |= __reduce_or_sync(
-            full, (entry && (wx & kWalkLeaf) && rel < (uint32_t)g.y) ? (1u << rel) : 0u);
+        if (entry && (wx & kWalkLeaf) && rel < (uint32_t)g.y) selfmask |= 1u << rel;
       }
       __syncwarp();
       if (wr - rd >= 32) {
-        group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, pi, a.eps2, ax2, ay2,
-                             az2);
+        group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi, a.eps2,
+                             ax2, ay2, az2);
         rd += 32;
         __syncwarp();
       }
@@ -1289,7 +1302,7 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
         const int f = __shfl_sync(full, w.z, src), c = __shfl_sync(full, cnt, src);
         if (COUNT) {
           const uint32_t o = (uint32_t)(k - f);
-          selfmask |= __ballot_sync(full, valid && o < (uint32_t)c);
+          if (valid && rr == 0 && o < (uint32_t)c) selfmask |= 1u << tl;
         }
         for (int b = 0; b < c; b += 32) {
           const bool e = b + lane < c;
@@ -1304,8 +1317,8 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
           wr += (uint32_t)min(32, c - b);
           __syncwarp();
           if (wr - rd >= 32) {
-            group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, pi, a.eps2, ax2,
-                                 ay2, az2);
+            group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi,
+                                 a.eps2, ax2, ay2, az2);
             rd += 32;
             __syncwarp();
           }
@@ -1328,12 +1341,19 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
       }
       __syncwarp();
       if (padded)
-        group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), padded, pi, a.eps2, ax2,
-                             ay2, az2);
+        group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), padded, rr, rep, pi,
+                             a.eps2, ax2, ay2, az2);
       __syncwarp();
     }
-    const int cnt_lane = (int)wr - (int)((selfmask >> lane) & 1u);
-    if (valid) {
+    for (int o = gw; o < 32; o <<= 1) {  // add up the replicas of each body
+      ax2 = f2_add(ax2, f2_shfl_xor(ax2, o));
+      ay2 = f2_add(ay2, f2_shfl_xor(ay2, o));
+      az2 = f2_add(az2, f2_shfl_xor(az2, o));
+    }
+    if (COUNT) selfmask = __reduce_or_sync(full, selfmask);
+    const int cnt_lane = (int)wr - (int)((selfmask >> tl) & 1u);
+    const bool owner = valid && rr == 0;
+    if (owner) {
       float sx0, sx1, sy0, sy1, sz0, sz1;
       f2_split(ax2, sx0, sx1);
       f2_split(ay2, sy0, sy1);
@@ -1345,7 +1365,7 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
       if (COUNT && a.counts) a.counts[i] = cnt_lane;
     }
     if (COUNT && a.inter_total) {
-      unsigned long long c = valid ? (unsigned long long)cnt_lane : 0ull;
+      unsigned long long c = owner ? (unsigned long long)cnt_lane : 0ull;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(full, c, o);
       if (lane == 0) atomicAdd(a.inter_total, c);

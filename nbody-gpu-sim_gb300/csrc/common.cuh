@@ -130,6 +130,11 @@ __device__ __forceinline__ f2 f2_fma(f2 a, f2 b, f2 c) {
   asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
   return r;
 }
+__device__ __forceinline__ f2 f2_shfl_xor(f2 a, int lane_mask) {
+  f2 r;
+  r.v = __shfl_xor_sync(0xffffffffu, a.v, lane_mask);
+  return r;
+}
 
 // ---------------------------------------------------------------------------
 // mbarrier + bulk copy (TMA, non-tensor form) helpers.

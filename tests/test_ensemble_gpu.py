@@ -93,11 +93,12 @@ def test_matches_plain_system_and_fp64_oracle(nb, orc):
         assert max(np.abs(got[k] - ref[k]).max() for k in ("vx", "vy", "vz")) <= 2e-4
 
 
-def test_bh_system_matches_plain_bh(nb):
+@pytest.mark.parametrize("group_walk", [0, 1])
+def test_bh_system_matches_plain_bh(nb, group_walk):
     s = nb.ics.plummer(12000, seed=31)
-    res, _ = _run(nb, {"b": (s, 30)}, direct_config=0)
+    res, _ = _run(nb, {"b": (s, 30)}, direct_config=0, group_walk=group_walk)
     got = res["b"][1]
-    calc = nb.BarnesHutCalculator(0.5)
+    calc = nb.BarnesHutCalculator(0.5, group_walk=bool(group_walk))
     calc.setSofteningParameter(0.01)
     sysm = nb.System(calc, s)
     sysm.step(1e-3, 30)
