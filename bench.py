@@ -50,7 +50,7 @@ L2_BYTES = 129 * 1024 * 1024
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60, help="timed engine ticks")
+    ap.add_argument("--steps", type=int, default=150, help="timed engine ticks")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="nbgb", choices=["nbgb", "reference"])
     ap.add_argument("--resident", type=int, default=96, help="resident systems at saturation")
@@ -151,7 +151,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
