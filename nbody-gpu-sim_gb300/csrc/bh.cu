@@ -1029,6 +1029,7 @@ constexpr int kGStack = 512;          // per-warp shared stack (nodes to test)
 constexpr int kGRing = 64;            // per-warp ring of pending list entries
 constexpr int kOvfChunk = 8704;       // per-warp stack overflow: 32 x 8 siblings x 34 levels
 constexpr int kOvfChunks = 256;       // overflow chunks per launch
+constexpr float kBoxWiden = 0x1.000004p0f;  // 1 + 2^-22: covers the half sizes' rounding
 
 struct GroupCounters {
   uint32_t ngroups;  // groups emitted by group_kernel
@@ -1159,7 +1160,7 @@ template <bool COUNT, bool ZERO_EPS>
 __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) {
   __shared__ int s_stack[8][kGStack];
   __shared__ __align__(16) float s_ring[8][4][kGRing];
-  __shared__ __align__(16) float4 s_box[8][2];  // group bounds: lo, hi
+  __shared__ __align__(16) float4 s_box[8][2];  // group box: centre, half sizes
   const uint32_t total = a.nstart[a.n];
   if ((int64_t)total > a.cap) return;  // the tree build failed and said so
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1191,9 +1192,15 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
       const float hix = float_of(__reduce_max_sync(full, ord_of(pi.x)));
       const float hiy = float_of(__reduce_max_sync(full, ord_of(pi.y)));
       const float hiz = float_of(__reduce_max_sync(full, ord_of(pi.z)));
-      if (lane == 0) {
-        s_box[wid][0] = make_float4(lox, loy, loz, 0.f);
-        s_box[wid][1] = make_float4(hix, hiy, hiz, 0.f);
+      if (lane == 0) {  // centre and half sizes, the halves widened past rounding
+        const float cx = __fmul_rn(__fadd_rn(lox, hix), 0.5f);
+        const float cy = __fmul_rn(__fadd_rn(loy, hiy), 0.5f);
+        const float cz = __fmul_rn(__fadd_rn(loz, hiz), 0.5f);
+        s_box[wid][0] = make_float4(cx, cy, cz, 0.f);
+        s_box[wid][1] = make_float4(
+            __fmul_rn(fmaxf(__fsub_rn(hix, cx), __fsub_rn(cx, lox)), kBoxWiden),
+            __fmul_rn(fmaxf(__fsub_rn(hiy, cy), __fsub_rn(cy, loy)), kBoxWiden),
+            __fmul_rn(fmaxf(__fsub_rn(hiz, cz), __fsub_rn(cz, loz)), kBoxWiden), 0.f);
       }
     }
     f2 ax2 = f2_make(0.f, 0.f), ay2 = ax2, az2 = ax2;
@@ -1255,16 +1262,15 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
           entry = cnt == 1;
           multi = cnt > 1;
         } else {
-          const float4 lo = s_box[wid][0], hi = s_box[wid][1];
-          const float lox = lo.x, loy = lo.y, loz = lo.z, hix = hi.x, hiy = hi.y, hiz = hi.z;
-          const bool overlap = __fsub_rn(ge.x, ge.w) <= hix && __fadd_rn(ge.x, ge.w) >= lox &&
-                               __fsub_rn(ge.y, ge.w) <= hiy && __fadd_rn(ge.y, ge.w) >= loy &&
-                               __fsub_rn(ge.z, ge.w) <= hiz && __fadd_rn(ge.z, ge.w) >= loz;
-          const float dx = fmaxf(fmaxf(__fsub_rn(lox, cm.x), __fsub_rn(cm.x, hix)), 0.0f);
-          const float dy = fmaxf(fmaxf(__fsub_rn(loy, cm.y), __fsub_rn(cm.y, hiy)), 0.0f);
-          const float dz = fmaxf(fmaxf(__fsub_rn(loz, cm.z), __fsub_rn(cm.z, hiz)), 0.0f);
-          const float d2 =
-              __fadd_rn(__fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx))), a.eps2);
+          const float4 bc = s_box[wid][0], bh = s_box[wid][1];
+          // cube and box touch / distance of the centre of mass outside the box
+          const bool overlap = fabsf(__fsub_rn(ge.x, bc.x)) <= __fadd_rn(ge.w, bh.x) &&
+                               fabsf(__fsub_rn(ge.y, bc.y)) <= __fadd_rn(ge.w, bh.y) &&
+                               fabsf(__fsub_rn(ge.z, bc.z)) <= __fadd_rn(ge.w, bh.z);
+          const float dx = fmaxf(__fsub_rn(fabsf(__fsub_rn(cm.x, bc.x)), bh.x), 0.0f);
+          const float dy = fmaxf(__fsub_rn(fabsf(__fsub_rn(cm.y, bc.y)), bh.y), 0.0f);
+          const float dz = fmaxf(__fsub_rn(fabsf(__fsub_rn(cm.z, bc.z)), bh.z), 0.0f);
+          const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
           entry = !overlap && __int_as_float(w.y) < __fmul_rn(a.theta2, d2);
           open = !entry;
         }

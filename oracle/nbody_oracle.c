@@ -595,13 +595,15 @@ int orc_bh_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* 
  * orc_bh_forces above).  Groups: the root if it holds at most 32 bodies;
  * below a larger node, runs of consecutive children (octant order) holding
  * at most 32 bodies in total, merged only when the parent holds at most 1024
- * bodies; a child of more than 32 bodies ends the run.  Each group walks the
- * tree once from the root: a node of zero mass is skipped, a leaf adds its
- * body, an internal node is accepted (its centre of mass added) when its
- * cube does not touch the group's bounding box (closed intervals, c -+ h
- * rounded) and 4h^2 < theta^2 * (fma(dz,dz, fma(dy,dy, dx*dx)) + eps^2),
- * d the per-axis distance of the centre of mass outside the box, else its
- * children are walked.  Every body of the group sums the whole list;
+ * bodies; a child of more than 32 bodies ends the run.  The group's box is
+ * its bounding box as a centre b = (lo + hi) * 0.5 and half sizes
+ * max(hi - b, b - lo) * (1 + 2^-22).  Each group walks the tree once from the
+ * root: a node of zero mass is skipped, a leaf adds its body, an internal
+ * node is accepted (its centre of mass added) unless its cube touches the
+ * box (|c - b| <= h + half on every axis) and when
+ * 4h^2 < theta^2 * fma(dz,dz, fma(dy,dy, fma(dx,dx, eps^2))), d the per-axis
+ * distance max(|com - b| - half, 0) of the centre of mass outside the box;
+ * otherwise its children are walked.  Every body of the group sums the whole list;
  * interactions per body = list length minus its own leaf.  With eps = 0 a
  * zero-distance entry adds nothing.  Multi-body (depth-32) leaves are not
  * supported here (their bodies are not listed in the node records):
@@ -685,6 +687,11 @@ int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const f
         if (p[a] > hi[a]) hi[a] = p[a];
       }
     }
+    float bc[3], bh[3];
+    for (int a = 0; a < 3; a++) {
+      bc[a] = (lo[a] + hi[a]) * 0.5f;
+      bh[a] = fmaxf(hi[a] - bc[a], bc[a] - lo[a]) * 0x1.000004p0f;
+    }
     /* interaction list */
     int cap = 4096, len = 0, own[ORC_GROUP] = {0};
     float* list = (float*)malloc(sizeof(float) * 4 * (size_t)cap);
@@ -700,13 +707,13 @@ int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const f
         for (int j = 0; j < nb; j++)
           if (body[j] == nd->particle_index) own[j] = 1;
       } else {
-        int overlap = nd->cx - nd->half <= hi[0] && nd->cx + nd->half >= lo[0] &&
-                      nd->cy - nd->half <= hi[1] && nd->cy + nd->half >= lo[1] &&
-                      nd->cz - nd->half <= hi[2] && nd->cz + nd->half >= lo[2];
-        float dx = fmaxf(fmaxf(lo[0] - nd->comx, nd->comx - hi[0]), 0.0f);
-        float dy = fmaxf(fmaxf(lo[1] - nd->comy, nd->comy - hi[1]), 0.0f);
-        float dz = fmaxf(fmaxf(lo[2] - nd->comz, nd->comz - hi[2]), 0.0f);
-        float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx)) + eps2;
+        int overlap = fabsf(nd->cx - bc[0]) <= nd->half + bh[0] &&
+                      fabsf(nd->cy - bc[1]) <= nd->half + bh[1] &&
+                      fabsf(nd->cz - bc[2]) <= nd->half + bh[2];
+        float dx = fmaxf(fabsf(nd->comx - bc[0]) - bh[0], 0.0f);
+        float dy = fmaxf(fabsf(nd->comy - bc[1]) - bh[1], 0.0f);
+        float dz = fmaxf(fabsf(nd->comz - bc[2]) - bh[2], 0.0f);
+        float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
         float size2 = 4.0f * nd->half * nd->half;
         entry = !overlap && size2 < theta2 * d2;
         if (!entry)
