@@ -1121,14 +1121,16 @@ __device__ __forceinline__ float float_of(uint32_t o) {
 // Adds list entries [base, base + cnt) of the ring (cnt a multiple of 4)
 // to the lane's target, two entries per packed operation.  With rep > 1
 // lanes of a small group, replica r of a body takes every rep-th quad.
-template <bool ZERO_EPS>
+template <bool ZERO_EPS, bool FULL>
 __device__ __forceinline__ void group_eval(const float* ex, const float* ey, const float* ez,
                                            const float* em, int base, int cnt, int r, int rep,
                                            float4 pi, float eps2, f2& ax2, f2& ay2, f2& az2) {
   const f2 px = f2_make(pi.x, pi.x), py = f2_make(pi.y, pi.y), pz = f2_make(pi.z, pi.z);
   const f2 e2 = f2_make(eps2, eps2);
-#pragma unroll 1
-  for (int j = 4 * r; j < cnt; j += 4 * rep) {
+  // FULL: one lane per body and a whole 32-entry chunk (fixed trip count)
+  const int j0 = FULL ? 0 : 4 * r, jn = FULL ? 32 : cnt, js = FULL ? 4 : 4 * rep;
+#pragma unroll(FULL ? 2 : 1)
+  for (int j = j0; j < jn; j += js) {
     const float4 X = *reinterpret_cast<const float4*>(ex + base + j);
     const float4 Y = *reinterpret_cast<const float4*>(ey + base + j);
     const float4 Z = *reinterpret_cast<const float4*>(ez + base + j);
@@ -1295,8 +1297,12 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
       }
       __syncwarp();
       if (wr - rd >= 32) {
-        group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi, a.eps2,
-                             ax2, ay2, az2);
+        if (rep == 1)
+          group_eval<ZERO_EPS, true>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, 0, 1, pi,
+                                     a.eps2, ax2, ay2, az2);
+        else
+          group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi,
+                                      a.eps2, ax2, ay2, az2);
         rd += 32;
         __syncwarp();
       }
@@ -1323,8 +1329,8 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
           wr += (uint32_t)min(32, c - b);
           __syncwarp();
           if (wr - rd >= 32) {
-            group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi,
-                                 a.eps2, ax2, ay2, az2);
+            group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi,
+                                        a.eps2, ax2, ay2, az2);
             rd += 32;
             __syncwarp();
           }
@@ -1347,8 +1353,8 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
       }
       __syncwarp();
       if (padded)
-        group_eval<ZERO_EPS>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), padded, rr, rep, pi,
-                             a.eps2, ax2, ay2, az2);
+        group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), padded, rr, rep, pi,
+                                    a.eps2, ax2, ay2, az2);
       __syncwarp();
     }
     for (int o = gw; o < 32; o <<= 1) {  // add up the replicas of each body
