@@ -40,8 +40,8 @@ import numpy as np  # noqa: E402
 METRIC = "batched vs plain particle-steps/s on 1 GB300 at stated force err; p99 latency"
 UNIT = "particle-steps/s"
 WORKLOAD = ("ensemble serving: Plummer clusters (a=1, M=1), N log-uniform [256, 65536], "
-            "steps U[100, 2000], eps=0.01, dt=1e-3, direct N<=8192 else Barnes-Hut theta=0.5 "
-            "(group walk), FP32 forces + FP64 state, 64 GiB admission budget")
+            "steps U[100, 2000], eps=0.01, dt=1e-3, direct N<=8192 else Barnes-Hut theta=0.5, "
+            "FP32 forces + FP64 state, 64 GiB admission budget")
 DT = 1e-3
 EPS = 0.01
 L2_BYTES = 129 * 1024 * 1024
@@ -559,7 +559,8 @@ def reference_arm(args, rank, world):
         "ms_per_step": 1e3 * tot_t / max(len(results), 1), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded Plummer clusters; no dataset)",
-        "config": {"workload": WORKLOAD, "path": "reference host CPU path (restated)"},
+        "config": {"workload": WORKLOAD, "path": "reference host CPU path (restated)",
+                   "bh_walk": "the reference's per-target walk on its insertion octree"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": orc.num_threads(),
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
