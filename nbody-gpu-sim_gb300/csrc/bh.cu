@@ -120,6 +120,7 @@ struct BHState {
   DevBuf<float4> spm;      // bodies in path order
   DevBuf<uint32_t> walk_ctr;  // next warp task of the walk
   DevBuf<int4> groups;        // group walk: first body, count, segment
+  bool groups_ready = false;  // the last build emitted groups
   DevBuf<char> group_ctr;     // group walk: GroupCounters
   DevBuf<int> group_ovf;      // group walk: stack overflow chunks
   int64_t n = 0;
@@ -587,25 +588,79 @@ __global__ void internal_nodes_kernel(EmitArgs a) {
   }
 }
 
+// Barnes-Hut group walk parameters (see the group walk below).
+constexpr int kGroupSize = 32;        // bodies per group (one per lane)
+constexpr int kGroupMergeMax = 1024;  // sibling subtrees merge only under parents this small
+constexpr int kGStack = 512;          // per-warp shared stack (nodes to test)
+constexpr int kGRing = 64;            // per-warp ring of pending list entries
+constexpr int kOvfChunk = 8704;       // per-warp stack overflow: 32 x 8 siblings x 34 levels
+constexpr int kOvfChunks = 256;       // overflow chunks per launch
+constexpr float kBoxWiden = 0x1.000004p0f;  // 1 + 2^-22: covers the half sizes' rounding
+
+struct GroupCounters {
+  uint32_t ngroups;  // groups emitted by link_kernel
+  uint32_t task;     // next group of the walk
+  uint32_t ovf;      // overflow chunks handed out
+  uint32_t pad;
+};
+
+// Where link_kernel writes the group walk's groups.
+struct GroupSink {
+  const uint32_t* body;  // path-sorted position -> concatenated body index
+  const int32_t* seg_of;
+  int4* groups;          // first body, count, segment
+  GroupCounters* gc;
+};
+
 // Parent links and child counts (children of P: P+1, skip(P+1), ... < skip(P)).
+// With GROUPS it also emits the group walk's groups: roots with at most
+// kGroupSize bodies; below larger nodes, runs of consecutive children with
+// at most kGroupSize bodies in total (merged only when the parent holds at
+// most kGroupMergeMax bodies: sibling cells of a large sparse node can lie
+// far apart); depth-32 leaves larger than a group are split.  Every body
+// belongs to exactly one group, and a group is one contiguous range of
+// path-sorted bodies.
+template <bool GROUPS>
 __global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __restrict__ nstart,
                             int64_t n, int64_t cap, int32_t* __restrict__ parent,
-                            int32_t* __restrict__ nchild) {
+                            int32_t* __restrict__ nchild, GroupSink gs) {
   const uint32_t total = nstart[n];
   if ((int64_t)total > cap) return;
+  auto emit = [&](int f, int c) {
+    const uint32_t g = atomicAdd(&gs.gc->ngroups, 1u);
+    gs.groups[g] = make_int4(f, c, gs.seg_of[gs.body[f]], 0);
+  };
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
        p += (int64_t)gridDim.x * blockDim.x) {
-    const int4 ip = nodes[p].info;
+    const int4 ip = nodes[p].info;  // skip, depth << 8 | leaf, first, count
     if (ip.y & 1) {
       nchild[p] = 0;
+      if (GROUPS && ip.w > kGroupSize)
+        for (int f = 0; f < ip.w; f += kGroupSize) emit(ip.z + f, min(kGroupSize, ip.w - f));
       continue;
     }
-    int c = (int)p + 1, nc = 0;
+    if (GROUPS && (ip.y >> 8) == 0 && ip.w <= kGroupSize) emit(ip.z, ip.w);  // a small root
+    const bool grp = GROUPS && ip.w > kGroupSize, merge = ip.w <= kGroupMergeMax;
+    int c = (int)p + 1, nc = 0, gf = 0, gn = 0;
     while (c < ip.x) {
       parent[c] = (int)p;
       ++nc;
-      c = nodes[c].info.x;
+      const int4 ci = nodes[c].info;
+      if (grp) {
+        if (ci.w > kGroupSize) {
+          if (gn) emit(gf, gn);
+          gn = 0;
+        } else if (gn && merge && gn + ci.w <= kGroupSize) {
+          gn += ci.w;
+        } else {
+          if (gn) emit(gf, gn);
+          gf = ci.z;
+          gn = ci.w;
+        }
+      }
+      c = ci.x;
     }
+    if (grp && gn) emit(gf, gn);
     nchild[p] = nc;
   }
 }
@@ -933,7 +988,7 @@ void bh_set_segments(BHState& h, const int64_t* off, const int64_t* n_per, int n
 
 // Builds the trees of all segments (positions and masses read from `pm` at
 // each segment's offset).
-void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err) {
+void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups) {
   const int64_t n = h.n;
   const int nseg = h.nseg;
   const size_t R = (size_t)h.reserve;  // per-body buffers are sized for the reserve
@@ -1006,8 +1061,16 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err) {
   NBGB_LAUNCH_CHECK();
   internal_nodes_kernel<<<grid1d(h.cap), 256, 0, st>>>(ea);
   NBGB_LAUNCH_CHECK();
-  link_kernel<<<grid1d(h.cap), 256, 0, st>>>(nodes, nst, n, h.cap, par, nch);
+  if (groups) {
+    GroupSink gs{h.body, h.seg_of.ptr, grow(h.groups, R),
+                 reinterpret_cast<GroupCounters*>(grow(h.group_ctr, sizeof(GroupCounters)))};
+    NBGB_CUDA(cudaMemsetAsync(gs.gc, 0, sizeof(GroupCounters), st));
+    link_kernel<true><<<grid1d(h.cap), 256, 0, st>>>(nodes, nst, n, h.cap, par, nch, gs);
+  } else {
+    link_kernel<false><<<grid1d(h.cap), 256, 0, st>>>(nodes, nst, n, h.cap, par, nch, GroupSink{});
+  }
   NBGB_LAUNCH_CHECK();
+  h.groups_ready = groups;
   com_kernel<<<grid1d(h.cap), 256, 0, st>>>(nodes, spm, nst, n, h.cap, par, nch, vis);
   NBGB_LAUNCH_CHECK();
 }
@@ -1023,68 +1086,6 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err) {
 // the group, so each target sees an equal or finer cell set than in the
 // reference walk.  Leaves contribute their bodies.  The list is evaluated by
 // all lanes at once, one target per lane, in packed FP32x2 arithmetic.
-constexpr int kGroupSize = 32;        // bodies per group (one per lane)
-constexpr int kGroupMergeMax = 1024;  // sibling subtrees merge only under parents this small
-constexpr int kGStack = 512;          // per-warp shared stack (nodes to test)
-constexpr int kGRing = 64;            // per-warp ring of pending list entries
-constexpr int kOvfChunk = 8704;       // per-warp stack overflow: 32 x 8 siblings x 34 levels
-constexpr int kOvfChunks = 256;       // overflow chunks per launch
-constexpr float kBoxWiden = 0x1.000004p0f;  // 1 + 2^-22: covers the half sizes' rounding
-
-struct GroupCounters {
-  uint32_t ngroups;  // groups emitted by group_kernel
-  uint32_t task;     // next group of the walk
-  uint32_t ovf;      // overflow chunks handed out
-  uint32_t pad;
-};
-
-// Groups: roots with at most kGroupSize bodies; below larger nodes, runs of
-// consecutive children with at most kGroupSize bodies in total (merged only
-// when the parent holds at most kGroupMergeMax bodies: sibling cells of a
-// large sparse node can lie far apart); multi-body leaves larger than a
-// group are split.  Every body belongs to exactly one group, and a group is
-// one contiguous range of path-sorted bodies.
-__global__ void group_kernel(const Node* __restrict__ nodes, const uint32_t* __restrict__ nstart,
-                             int64_t n, int64_t cap, const uint32_t* __restrict__ body,
-                             const int32_t* __restrict__ seg_of, int4* __restrict__ groups,
-                             GroupCounters* __restrict__ gc) {
-  const uint32_t total = nstart[n];
-  if ((int64_t)total > cap) return;
-  auto emit = [&](int f, int c) {
-    const uint32_t g = atomicAdd(&gc->ngroups, 1u);
-    groups[g] = make_int4(f, c, seg_of[body[f]], 0);
-  };
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    const int4 in = nodes[p].info;  // skip, depth << 8 | leaf, first, count
-    if (in.w <= kGroupSize) {
-      if ((in.y >> 8) == 0) emit(in.z, in.w);  // a segment root
-      continue;
-    }
-    if (in.y & 1) {  // depth-32 leaf holding more bodies than a group
-      for (int f = 0; f < in.w; f += kGroupSize) emit(in.z + f, min(kGroupSize, in.w - f));
-      continue;
-    }
-    const bool merge = in.w <= kGroupMergeMax;
-    int gf = 0, gn = 0;
-    for (int c = (int)p + 1; c < in.x;) {
-      const int4 ci = nodes[c].info;
-      if (ci.w > kGroupSize) {
-        if (gn) emit(gf, gn);
-        gn = 0;
-      } else if (gn && merge && gn + ci.w <= kGroupSize) {
-        gn += ci.w;
-      } else {
-        if (gn) emit(gf, gn);
-        gf = ci.z;
-        gn = ci.w;
-      }
-      c = ci.x;
-    }
-    if (gn) emit(gf, gn);
-  }
-}
-
 struct GroupWalkArgs {
   const Node* nodes;
   const float4* spm;
@@ -1425,13 +1426,13 @@ static void bh_group_walk(BHState& h, const BHWalkParams& p, float* ax, float* a
                           int32_t* counts, unsigned long long* inter_total, uint32_t* err,
                           cudaStream_t st) {
   const int64_t n = h.n;
-  int4* groups = grow(h.groups, (size_t)h.reserve);
-  GroupCounters* gc = reinterpret_cast<GroupCounters*>(grow(h.group_ctr, sizeof(GroupCounters)));
+  if (!h.groups_ready)
+    fail(NBGB_ERR_INVALID_ARG, "Barnes-Hut group walk without groups from the tree build");
+  int4* groups = h.groups.ptr;
+  GroupCounters* gc = reinterpret_cast<GroupCounters*>(h.group_ctr.ptr);
   int* ovf = grow(h.group_ovf, (size_t)kOvfChunks * kOvfChunk);
-  NBGB_CUDA(cudaMemsetAsync(gc, 0, sizeof(GroupCounters), st));
-  group_kernel<<<grid1d(h.cap), 256, 0, st>>>(h.nodes.ptr, h.nstart.ptr, n, h.cap, h.body,
-                                              h.seg_of.ptr, groups, gc);
-  NBGB_LAUNCH_CHECK();
+  // the walk's task and overflow counters (the group count stays)
+  NBGB_CUDA(cudaMemsetAsync(&gc->task, 0, 2 * sizeof(uint32_t), st));
   GroupWalkArgs g;
   g.nodes = h.nodes.ptr;
   g.spm = h.spm.ptr;
@@ -1544,7 +1545,7 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
   const bool sync = (c->params.flags & NBGB_FLAG_SYNC) != 0;
   if (!sync) bh_reserve_async(h);
   for (int attempt = 0; attempt < 2; ++attempt) {
-    bh_build(h, pm, st, err);
+    bh_build(h, pm, st, err, (c->params.flags & NBGB_FLAG_GROUP_WALK) != 0);
     if (!sync) break;  // capacity overflow surfaces through the device error word
     // The node count is data dependent: read it back and regrow once if the
     // capacity was too small (the kernels skipped their work in that case).

@@ -42,8 +42,9 @@ void bh_set_segments(BHState& h, const int64_t* off, const int64_t* n_per, int n
                      cudaStream_t st, char* staging);
 // Node capacity for use without a read-back (4 nodes per body + 64 per segment).
 void bh_reserve_async(BHState& h);
-// Trees of all segments (bit-identical, per segment, to the single-system tree).
-void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err);
+// Trees of all segments (bit-identical, per segment, to the single-system tree);
+// `groups` also emits the group walk's groups.
+void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups);
 // Accelerations of all segments, written at each segment's offset into
 // ax/ay/az.  counts (per arena index) and inter_total (running sum) are
 // optional; err receives device error bits (group walk stack overflow).

@@ -486,12 +486,12 @@ static int64_t run_bh_pass(nbgb_ensemble* e) {
     NBGB_CUDA(cudaGraphLaunch(e->bh_exec, e->bh_stream));
     graph_kernels = e->bh_graph_kernels;
   } else if (!e->cfg.use_graphs || e->bh_stable < 1) {
-    bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr);
+    bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr, e->cfg.group_walk != 0);
   } else {
     const int64_t l0 = t_launches;
     NBGB_CUDA(cudaStreamBeginCapture(e->bh_stream, cudaStreamCaptureModeThreadLocal));
     try {
-      bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr);
+      bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr, e->cfg.group_walk != 0);
     } catch (...) {
       cudaGraph_t g = nullptr;
       cudaStreamEndCapture(e->bh_stream, &g);
