@@ -1071,7 +1071,10 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   }
   NBGB_LAUNCH_CHECK();
   h.groups_ready = groups;
-  com_kernel<<<grid1d(h.cap), 256, 0, st>>>(nodes, spm, nst, n, h.cap, par, nch, vis);
+  // one thread per node slot: a leaf thread carries centres of mass up the
+  // tree, so slots are not chained per thread
+  com_kernel<<<(unsigned)ceil_div(h.cap, 256), 256, 0, st>>>(nodes, spm, nst, n, h.cap, par, nch,
+                                                            vis);
   NBGB_LAUNCH_CHECK();
 }
 
