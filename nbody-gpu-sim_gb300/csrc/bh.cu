@@ -1131,34 +1131,31 @@ __device__ __forceinline__ void group_eval(const float* ex, const float* ey, con
                                            float4 pi, float eps2, f2& ax2, f2& ay2, f2& az2) {
   const f2 px = f2_make(pi.x, pi.x), py = f2_make(pi.y, pi.y), pz = f2_make(pi.z, pi.z);
   const f2 e2 = f2_make(eps2, eps2);
-  // FULL: one lane per body and a whole 32-entry chunk (fixed trip count)
-  const int j0 = FULL ? 0 : 4 * r, jn = FULL ? 32 : cnt, js = FULL ? 4 : 4 * rep;
-#pragma unroll(FULL ? 2 : 1)
+  // FULL: one lane per body and a whole 32-entry chunk (fixed trip count);
+  // entries are read as pairs straight into packed registers
+  const int j0 = FULL ? 0 : 2 * r, jn = FULL ? 32 : cnt, js = FULL ? 2 : 2 * rep;
+#pragma unroll(FULL ? 4 : 1)
   for (int j = j0; j < jn; j += js) {
-    const float4 X = *reinterpret_cast<const float4*>(ex + base + j);
-    const float4 Y = *reinterpret_cast<const float4*>(ey + base + j);
-    const float4 Z = *reinterpret_cast<const float4*>(ez + base + j);
-    const float4 M = *reinterpret_cast<const float4*>(em + base + j);
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const f2 dx = f2_sub(h ? f2_make(X.z, X.w) : f2_make(X.x, X.y), px);
-      const f2 dy = f2_sub(h ? f2_make(Y.z, Y.w) : f2_make(Y.x, Y.y), py);
-      const f2 dz = f2_sub(h ? f2_make(Z.z, Z.w) : f2_make(Z.x, Z.y), pz);
-      const f2 d2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, e2)));
-      float d2l, d2h;
-      f2_split(d2, d2l, d2h);
-      float rl = rsqrt_approx(d2l), rh = rsqrt_approx(d2h);
-      if (ZERO_EPS) {  // coincident bodies (and the target itself) add nothing
-        rl = d2l > 0.0f ? rl : 0.0f;
-        rh = d2h > 0.0f ? rh : 0.0f;
-      }
-      const f2 r = f2_make(rl, rh);
-      const f2 m = h ? f2_make(M.z, M.w) : f2_make(M.x, M.y);
-      const f2 f = f2_mul(f2_mul(m, r), f2_mul(r, r));
-      ax2 = f2_fma(f, dx, ax2);
-      ay2 = f2_fma(f, dy, ay2);
-      az2 = f2_fma(f, dz, az2);
+    const f2 xj{*reinterpret_cast<const unsigned long long*>(ex + base + j)};
+    const f2 yj{*reinterpret_cast<const unsigned long long*>(ey + base + j)};
+    const f2 zj{*reinterpret_cast<const unsigned long long*>(ez + base + j)};
+    const f2 m{*reinterpret_cast<const unsigned long long*>(em + base + j)};
+    const f2 dx = f2_sub(xj, px);
+    const f2 dy = f2_sub(yj, py);
+    const f2 dz = f2_sub(zj, pz);
+    const f2 d2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, e2)));
+    float d2l, d2h;
+    f2_split(d2, d2l, d2h);
+    float rl = rsqrt_approx(d2l), rh = rsqrt_approx(d2h);
+    if (ZERO_EPS) {  // coincident bodies (and the target itself) add nothing
+      rl = d2l > 0.0f ? rl : 0.0f;
+      rh = d2h > 0.0f ? rh : 0.0f;
     }
+    const f2 rr = f2_make(rl, rh);
+    const f2 f = f2_mul(f2_mul(m, rr), f2_mul(rr, rr));
+    ax2 = f2_fma(f, dx, ax2);
+    ay2 = f2_fma(f, dy, ay2);
+    az2 = f2_fma(f, dz, az2);
   }
 }
 
