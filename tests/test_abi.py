@@ -39,6 +39,13 @@ def test_abi_version_and_defaults(nb):
         (1.0, pytest.approx(0.1), 0.5, 2.0, 2.0, 256)
     assert p.leaf_capacity == 1
     assert p.flags & nb.FLAG_SYNC and p.flags & nb.FLAG_COMPENSATED
+    # the drop-in calculator walks the tree as the reference does; the
+    # serving engine defaults to the group walk
+    assert not p.flags & nb.FLAG_GROUP_WALK
+    assert nb.BarnesHutCalculator.__init__.__defaults__[-1] is False  # group_walk
+    from nbgb.serving import default_config
+    cfg = default_config()
+    assert cfg.group_walk == 1 and cfg.leaf_capacity == 1 and cfg.theta == 0.5
 
 
 def test_struct_layouts_match_reference(nb):
