@@ -62,3 +62,11 @@ def test_struct_layouts_match_reference(nb):
 def test_method_enum_matches_reference(nb):
     assert [int(m) for m in nb.ForceMethod] == [0, 1, 2]
     assert nb.forceMethodToString(nb.ForceMethod.BARNES_HUT) == "barnes_hut"
+
+
+def test_group_walk_stack_hook_validates(nb):
+    # process-wide test hook of the group walk; no device work
+    lib = nb.lib()
+    assert lib.nbgb_selftest_group_walk_stack(63) == 1  # NBGB_ERR_INVALID_ARG
+    assert lib.nbgb_selftest_group_walk_stack(513) == 1
+    assert lib.nbgb_selftest_group_walk_stack(512) == 0  # the default
