@@ -1088,7 +1088,8 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
 // reference's per-target test (force_barnes_hut.cu:218-224) for every body of
 // the group, so each target sees an equal or finer cell set than in the
 // reference walk.  Leaves contribute their bodies.  The list is evaluated by
-// all lanes at once, one target per lane, in packed FP32x2 arithmetic.
+// all lanes at once, one target per lane (2 or 4 lanes per target in groups
+// of at most 16 or 8 bodies), in packed FP32x2 arithmetic.
 struct GroupWalkArgs {
   const Node* nodes;
   const float4* spm;
@@ -1124,7 +1125,7 @@ __device__ __forceinline__ float float_of(uint32_t o) {
 
 // Adds list entries [base, base + cnt) of the ring (cnt a multiple of 4)
 // to the lane's target, two entries per packed operation.  With rep > 1
-// lanes of a small group, replica r of a body takes every rep-th quad.
+// lanes per body (small groups), replica r takes every rep-th pair.
 template <bool ZERO_EPS, bool FULL>
 __device__ __forceinline__ void group_eval(const float* ex, const float* ey, const float* ez,
                                            const float* em, int base, int cnt, int r, int rep,
