@@ -62,6 +62,7 @@ struct Options {
   std::string export_path;
   std::string import_path;
   std::string export_initial_path;
+  bool group_walk = false;  // extension: --bh-walk group
 };
 
 const char* method_name(int m) {  // forceMethodToString (types.hpp:39-49)
@@ -158,6 +159,14 @@ Options parse(int argc, char** argv) {
       o.import_path = require_value(argc, argv, i, a);
     } else if (a == "--export-initial") {
       o.export_initial_path = require_value(argc, argv, i, a);
+    } else if (a == "--bh-walk") {
+      const std::string v = require_value(argc, argv, i, a);
+      if (v == "group")
+        o.group_walk = true;
+      else if (v == "reference")
+        o.group_walk = false;
+      else
+        throw ValidationError("Unsupported Barnes-Hut walk: " + v);
     } else if (!a.empty() && a.front() == '-') {
       throw ValidationError("Unknown argument: " + a);
     } else {
@@ -187,6 +196,7 @@ std::string usage() {
     << "  --theta VALUE          Set Barnes-Hut theta\n"
     << "  --cell-size VALUE      Set spatial hash cell size\n"
     << "  --cutoff VALUE         Set spatial hash cutoff radius\n"
+    << "  --bh-walk NAME         reference | group (Barnes-Hut walk; default reference)\n"
     << "  --benchmark            Run a non-interactive benchmark and exit\n"
     << "  --benchmark-steps N    Set benchmark update steps\n"
     << "  --benchmark-output P   Write benchmark JSON to path P\n"
@@ -362,6 +372,7 @@ int run_benchmark(const Options& o) {
   p.theta = o.theta;
   p.cell_size = o.cell_size;
   p.cutoff = o.cutoff;
+  if (o.group_walk && s.force_method == NBGB_BARNES_HUT) p.flags |= NBGB_FLAG_GROUP_WALK;
   nbgb_calculator* calc = nullptr;
   check(nbgb_calculator_create((nbgb_method)s.force_method, &p, &calc));
   nbgb_system* sys = nullptr;
@@ -397,6 +408,7 @@ int run_benchmark(const Options& o) {
   params["particle_count"] = (double)o.particle_count;
   if (o.force_method == NBGB_BARNES_HUT) {
     params["theta"] = o.theta;
+    if (o.group_walk) params["group_walk"] = 1;
   } else if (o.force_method == NBGB_SPATIAL_HASH) {
     params["cell_size"] = o.cell_size;
     params["cutoff_radius"] = o.cutoff;

@@ -33,7 +33,7 @@ def _run(app, *args):
 
 def test_help(app):
     r = _run(app, "--help")
-    assert r.returncode == 0 and "--benchmark-output P" in r.stdout
+    assert r.returncode == 0 and "--benchmark-output P" in r.stdout and "--bh-walk" in r.stdout
 
 
 @pytest.mark.parametrize("args,msg", [
@@ -47,6 +47,7 @@ def test_help(app):
     (("--theta", "3"), "Validation Error: Barnes-Hut theta must be between 0 and 2"),
     (("--particles", "0"), "Validation Error: Particle count must be greater than 0"),
     (("--benchmark-steps", "0"), "Validation Error: Benchmark steps must be greater than zero"),
+    (("--bh-walk", "sideways"), "Validation Error: Unsupported Barnes-Hut walk: sideways"),
 ])
 def test_cli_validation(app, args, msg):
     r = _run(app, *args)

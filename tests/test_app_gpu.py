@@ -74,3 +74,10 @@ def test_export_import_roundtrip_and_trajectory(app, tmp_path, nb):
     for k in ("x", "y", "z", "vx", "vy", "vz"):
         np.testing.assert_array_equal(s1[k], st[k])
     assert np.abs(s2["x"] - s1["x"]).max() > 0  # it moved on after the import
+
+
+def test_group_walk_option(app, tmp_path):
+    r = _run(app, "--benchmark", "--particles", "20000", "--benchmark-steps", "3", "--method",
+             "barnes-hut", "--bh-walk", "group")
+    b = json.loads(r.stdout.strip().splitlines()[-1])["benchmarks"][0]
+    assert b["parameters"]["group_walk"] == 1 and b["metrics"]["wall_time_ms"] > 0
