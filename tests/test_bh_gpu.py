@@ -160,7 +160,8 @@ def _gen(nb, gen, n):
 @pytest.mark.parametrize("gen,n,theta,eps", [("plummer", 5000, 0.5, 0.01), ("plummer", 20000, 0.3, 0.01),
                                              ("two", 50000, 0.5, 0.01), ("cube", 30000, 0.5, 0.01),
                                              ("far", 6000, 0.5, 0.01), ("dense", 6000, 0.5, 0.01),
-                                             ("plummer", 3000, 1.0, 0.01), ("plummer", 4000, 0.5, 0.0)])
+                                             ("plummer", 3000, 1.0, 0.01), ("plummer", 4000, 0.5, 0.0),
+                                             ("plummer", 3000, 2.0, 0.01), ("cube", 5000, 0.5, 5.0)])
 def test_group_walk_matches_oracle(nb, orc, gen, n, theta, eps):
     """Group walk: per-body list lengths (interactions) equal the oracle's
     group walk on the same tree -- same groups, same bounding boxes, same
