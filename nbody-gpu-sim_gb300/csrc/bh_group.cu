@@ -1,0 +1,396 @@
+// bh_group.cu -- the Barnes-Hut group walk (NBGB_FLAG_GROUP_WALK): one
+// interaction list per group of at most 32 nearby bodies, built by one warp
+// that tests 32 nodes at a time and evaluated by all its lanes.  Groups come
+// from the tree build (link_kernel in bh.cu).
+#include <algorithm>
+#include <atomic>
+
+#include "bh_tree.cuh"
+#include "kernels.cuh"
+
+namespace nbgb {
+
+// ---------------------------------------------------------- group walk --
+// Barnes-Hut with a per-group opening test: the bodies of one small subtree
+// (or of consecutive small sibling subtrees, at most 32 bodies) share one
+// interaction list, built by one warp that tests 32 nodes at a time.  A cell
+// is accepted for the whole group when its cube does not touch the group's
+// bounding box and size2 < theta2 (d_min^2 + eps^2), d_min being the distance
+// from the cell's centre of mass to the box: every accepted cell passes the
+// reference's per-target test (force_barnes_hut.cu:218-224) for every body of
+// the group, so each target sees an equal or finer cell set than in the
+// reference walk.  Leaves contribute their bodies.  The list is evaluated by
+// all lanes at once, one target per lane (2 or 4 lanes per target in groups
+// of at most 16 or 8 bodies), in packed FP32x2 arithmetic.
+struct GroupWalkArgs {
+  const Node* nodes;
+  const float4* spm;
+  const uint32_t* body;
+  const uint32_t* nstart;
+  SegView sv;
+  const int4* groups;
+  const int32_t* seg_root;
+  int64_t n;
+  int64_t cap;
+  float theta2;
+  float eps2;
+  float G;
+  float* ax;
+  float* ay;
+  float* az;
+  int32_t* counts;                  // per-body list lengths without the body itself (or null)
+  unsigned long long* inter_total;  // sum of counts (or null)
+  GroupCounters* gc;
+  int* ovf;                         // kOvfChunks x kOvfChunk stack overflow entries
+  uint32_t* err;
+  int stack_limit;                  // shared stack entries used (64 .. kGStack)
+};
+
+// Floats as unsigned integers with the same order (finite values).
+__device__ __forceinline__ uint32_t ord_of(float f) {
+  const uint32_t u = __float_as_uint(f);
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float float_of(uint32_t o) {
+  return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+// Adds list entries [base, base + cnt) of the ring (cnt a multiple of 4)
+// to the lane's target, two entries per packed operation.  With rep > 1
+// lanes per body (small groups), replica r takes every rep-th pair.
+template <bool ZERO_EPS, bool FULL>
+__device__ __forceinline__ void group_eval(const float* ex, const float* ey, const float* ez,
+                                           const float* em, int base, int cnt, int r, int rep,
+                                           float4 pi, float eps2, f2& ax2, f2& ay2, f2& az2) {
+  const f2 px = f2_make(pi.x, pi.x), py = f2_make(pi.y, pi.y), pz = f2_make(pi.z, pi.z);
+  const f2 e2 = f2_make(eps2, eps2);
+  // FULL: one lane per body and a whole 32-entry chunk (fixed trip count);
+  // entries are read as pairs straight into packed registers
+  const int j0 = FULL ? 0 : 2 * r, jn = FULL ? 32 : cnt, js = FULL ? 2 : 2 * rep;
+#pragma unroll(FULL ? 4 : 1)
+  for (int j = j0; j < jn; j += js) {
+    const f2 xj{*reinterpret_cast<const unsigned long long*>(ex + base + j)};
+    const f2 yj{*reinterpret_cast<const unsigned long long*>(ey + base + j)};
+    const f2 zj{*reinterpret_cast<const unsigned long long*>(ez + base + j)};
+    const f2 m{*reinterpret_cast<const unsigned long long*>(em + base + j)};
+    const f2 dx = f2_sub(xj, px);
+    const f2 dy = f2_sub(yj, py);
+    const f2 dz = f2_sub(zj, pz);
+    const f2 d2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, e2)));
+    float d2l, d2h;
+    f2_split(d2, d2l, d2h);
+    float rl = rsqrt_approx(d2l), rh = rsqrt_approx(d2h);
+    if (ZERO_EPS) {  // coincident bodies (and the target itself) add nothing
+      rl = d2l > 0.0f ? rl : 0.0f;
+      rh = d2h > 0.0f ? rh : 0.0f;
+    }
+    const f2 rr = f2_make(rl, rh);
+    const f2 f = f2_mul(f2_mul(m, rr), f2_mul(rr, rr));
+    ax2 = f2_fma(f, dx, ax2);
+    ay2 = f2_fma(f, dy, ay2);
+    az2 = f2_fma(f, dz, az2);
+  }
+}
+
+template <bool COUNT, bool ZERO_EPS>
+__global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) {
+  __shared__ int s_stack[8][kGStack];
+  __shared__ __align__(16) float s_ring[8][4][kGRing];
+  __shared__ __align__(16) float4 s_box[8][2];  // group box: centre, half sizes
+  const uint32_t total = a.nstart[a.n];
+  if ((int64_t)total > a.cap) return;  // the tree build failed and said so
+  const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned full = 0xffffffffu, lt = (1u << lane) - 1u;
+  int* stk = s_stack[wid];
+  float* ex = s_ring[wid][0];
+  float* ey = s_ring[wid][1];
+  float* ez = s_ring[wid][2];
+  float* em = s_ring[wid][3];
+  const uint32_t ngroups = *(volatile uint32_t*)&a.gc->ngroups;
+  int* ovf = nullptr;  // this warp's overflow chunk, taken on first use
+  while (true) {
+    uint32_t t32 = 0;
+    if (lane == 0) t32 = atomicAdd(&a.gc->task, 1u);
+    const uint32_t t = __shfl_sync(full, t32, 0);
+    if (t >= ngroups) break;
+    const int4 g = a.groups[t];  // first, count, segment
+    // a group of at most 8 (16) bodies gives each body 4 (2) lanes, each
+    // summing a share of the list: lane = replica * gw + body
+    const int gw = g.y <= 8 ? 8 : (g.y <= 16 ? 16 : 32);
+    const int rep = 32 / gw, tl = lane & (gw - 1), rr = lane / gw;
+    const bool valid = tl < g.y;
+    const int k = g.x + (valid ? tl : 0);
+    const float4 pi = a.spm[k];
+    {
+      const float lox = float_of(__reduce_min_sync(full, ord_of(pi.x)));
+      const float loy = float_of(__reduce_min_sync(full, ord_of(pi.y)));
+      const float loz = float_of(__reduce_min_sync(full, ord_of(pi.z)));
+      const float hix = float_of(__reduce_max_sync(full, ord_of(pi.x)));
+      const float hiy = float_of(__reduce_max_sync(full, ord_of(pi.y)));
+      const float hiz = float_of(__reduce_max_sync(full, ord_of(pi.z)));
+      if (lane == 0) {  // centre and half sizes, the halves widened past rounding
+        const float cx = __fmul_rn(__fadd_rn(lox, hix), 0.5f);
+        const float cy = __fmul_rn(__fadd_rn(loy, hiy), 0.5f);
+        const float cz = __fmul_rn(__fadd_rn(loz, hiz), 0.5f);
+        s_box[wid][0] = make_float4(cx, cy, cz, 0.f);
+        s_box[wid][1] = make_float4(
+            __fmul_rn(fmaxf(__fsub_rn(hix, cx), __fsub_rn(cx, lox)), kBoxWiden),
+            __fmul_rn(fmaxf(__fsub_rn(hiy, cy), __fsub_rn(cy, loy)), kBoxWiden),
+            __fmul_rn(fmaxf(__fsub_rn(hiz, cz), __fsub_rn(cz, loz)), kBoxWiden), 0.f);
+      }
+    }
+    f2 ax2 = f2_make(0.f, 0.f), ay2 = ax2, az2 = ax2;
+    uint32_t wr = 0, rd = 0;  // list entries written / evaluated
+    uint32_t selfmask = 0;    // bodies (by index in the group) whose own leaf is in the list
+    int sp = 1, gsp = 0;
+    bool failed = false;
+    if (lane == 0) stk[0] = a.seg_root[g.z];
+    __syncwarp();
+    while (sp > 0 || gsp > 0) {
+      if (sp == 0) {  // refill from the overflow chunk
+        const int m = min(gsp, a.stack_limit / 2);
+        for (int j = lane; j < m; j += 32) stk[j] = ovf[gsp - m + j];
+        gsp -= m;
+        sp = m;
+        __syncwarp();
+      }
+      if (sp > a.stack_limit - 32) {  // a step adds at most 32: spill the oldest half
+        const int half = a.stack_limit / 2;
+        if (!ovf) {
+          uint32_t c32 = 0;
+          if (lane == 0) c32 = atomicAdd(&a.gc->ovf, 1u);
+          const uint32_t c = __shfl_sync(full, c32, 0);
+          if (c < (uint32_t)kOvfChunks) ovf = a.ovf + (size_t)c * kOvfChunk;
+        }
+        if (!ovf || gsp + half > kOvfChunk) {
+          failed = true;
+          break;
+        }
+        for (int j = lane; j < half; j += 32) ovf[gsp + j] = stk[j];
+        __syncwarp();
+        for (int j = lane; j < sp - half; j += 32) stk[j] = stk[half + j];
+        gsp += half;
+        sp -= half;
+        __syncwarp();
+      }
+      const int m = min(sp, 32);
+      sp -= m;
+      const bool have = lane < m;
+      const int node = have ? stk[sp + lane] : 0;
+      __syncwarp();
+      f2 cm_xy = f2_make(0.f, 0.f), cm_zw = cm_xy, g_xy = cm_xy, g_zw = cm_xy;
+      int4 w = make_int4((int)kWalkZero, 0, 0, 0);
+      if (have) {
+        ld_node2(&a.nodes[node], cm_xy, cm_zw, g_xy, g_zw);
+        w = __ldg(&a.nodes[node].walk);
+      }
+      float4 cm, ge;
+      f2_split(cm_xy, cm.x, cm.y);
+      f2_split(cm_zw, cm.z, cm.w);
+      f2_split(g_xy, ge.x, ge.y);
+      f2_split(g_zw, ge.z, ge.w);
+      const uint32_t wx = (uint32_t)w.x;
+      const bool next = have && ((uint32_t)w.w & kWalkNext);
+      const int cnt = (int)((uint32_t)w.w & ~kWalkNext);
+      bool entry = false, open = false, multi = false;
+      if (!(wx & kWalkZero)) {
+        if (wx & kWalkLeaf) {
+          entry = cnt == 1;
+          multi = cnt > 1;
+        } else {
+          const float4 bc = s_box[wid][0], bh = s_box[wid][1];
+          // cube and box touch / distance of the centre of mass outside the box
+          const bool overlap = fabsf(__fsub_rn(ge.x, bc.x)) <= __fadd_rn(ge.w, bh.x) &&
+                               fabsf(__fsub_rn(ge.y, bc.y)) <= __fadd_rn(ge.w, bh.y) &&
+                               fabsf(__fsub_rn(ge.z, bc.z)) <= __fadd_rn(ge.w, bh.z);
+          const float dx = fmaxf(__fsub_rn(fabsf(__fsub_rn(cm.x, bc.x)), bh.x), 0.0f);
+          const float dy = fmaxf(__fsub_rn(fabsf(__fsub_rn(cm.y, bc.y)), bh.y), 0.0f);
+          const float dz = fmaxf(__fsub_rn(fabsf(__fsub_rn(cm.z, bc.z)), bh.z), 0.0f);
+          const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
+          entry = !overlap && __int_as_float(w.y) < __fmul_rn(a.theta2, d2);
+          open = !entry;
+        }
+      }
+      // next siblings below first children, so the walk goes depth first
+      const unsigned bs = __ballot_sync(full, next), bo = __ballot_sync(full, open);
+      if (next) stk[sp + __popc(bs & lt)] = (int)(wx & (kWalkZero - 1u));
+      if (open) stk[sp + __popc(bs) + __popc(bo & lt)] = node + 1;
+      sp += __popc(bs) + __popc(bo);
+      const unsigned be = __ballot_sync(full, entry);
+      if (entry) {
+        const int slot = (int)((wr + __popc(be & lt)) & (kGRing - 1));
+        ex[slot] = cm.x;
+        ey[slot] = cm.y;
+        ez[slot] = cm.z;
+        em[slot] = cm.w;
+      }
+      wr += __popc(be);
+      if (COUNT) {  // lane-local here, combined over the warp at the end
+        const uint32_t rel = (uint32_t)(w.z - g.x);
+        if (entry && (wx & kWalkLeaf) && rel < (uint32_t)g.y) selfmask |= 1u << rel;
+      }
+      __syncwarp();
+      if (wr - rd >= 32) {
+        if (rep == 1)
+          group_eval<ZERO_EPS, true>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, 0, 1, pi,
+                                     a.eps2, ax2, ay2, az2);
+        else
+          group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi,
+                                      a.eps2, ax2, ay2, az2);
+        rd += 32;
+        __syncwarp();
+      }
+      // multi-body (depth-32) leaves: their bodies one by one
+      unsigned bm = __ballot_sync(full, multi);
+      while (bm) {
+        const int src = __ffs(bm) - 1;
+        bm &= bm - 1;
+        const int f = __shfl_sync(full, w.z, src), c = __shfl_sync(full, cnt, src);
+        if (COUNT) {
+          const uint32_t o = (uint32_t)(k - f);
+          if (valid && rr == 0 && o < (uint32_t)c) selfmask |= 1u << tl;
+        }
+        for (int b = 0; b < c; b += 32) {
+          const bool e = b + lane < c;
+          if (e) {
+            const float4 q = a.spm[f + b + lane];
+            const int slot = (int)((wr + lane) & (kGRing - 1));
+            ex[slot] = q.x;
+            ey[slot] = q.y;
+            ez[slot] = q.z;
+            em[slot] = q.w;
+          }
+          wr += (uint32_t)min(32, c - b);
+          __syncwarp();
+          if (wr - rd >= 32) {
+            group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi,
+                                        a.eps2, ax2, ay2, az2);
+            rd += 32;
+            __syncwarp();
+          }
+        }
+      }
+    }
+    if (failed) {
+      if (lane == 0) raise_error(a.err, kErrWalkStack);
+      const float nan = __int_as_float(0x7fc00000);
+      ax2 = ay2 = az2 = f2_make(nan, nan);
+    } else {
+      // the rest of the list, padded to a multiple of 4 with massless entries
+      const int left = (int)(wr - rd), padded = (left + 3) & ~3;
+      if (lane >= left && lane < padded) {
+        const int slot = (int)((rd + lane) & (kGRing - 1));
+        ex[slot] = 3.0e18f;
+        ey[slot] = 0.0f;
+        ez[slot] = 0.0f;
+        em[slot] = 0.0f;
+      }
+      __syncwarp();
+      if (padded)
+        group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), padded, rr, rep, pi,
+                                    a.eps2, ax2, ay2, az2);
+      __syncwarp();
+    }
+    for (int o = gw; o < 32; o <<= 1) {  // add up the replicas of each body
+      ax2 = f2_add(ax2, f2_shfl_xor(ax2, o));
+      ay2 = f2_add(ay2, f2_shfl_xor(ay2, o));
+      az2 = f2_add(az2, f2_shfl_xor(az2, o));
+    }
+    if (COUNT) selfmask = __reduce_or_sync(full, selfmask);
+    const int cnt_lane = (int)wr - (int)((selfmask >> tl) & 1u);
+    const bool owner = valid && rr == 0;
+    if (owner) {
+      float sx0, sx1, sy0, sy1, sz0, sz1;
+      f2_split(ax2, sx0, sx1);
+      f2_split(ay2, sy0, sy1);
+      f2_split(az2, sz0, sz1);
+      const int64_t i = a.sv.arena(a.body[k]);
+      a.ax[i] = a.G * (sx0 + sx1);
+      a.ay[i] = a.G * (sy0 + sy1);
+      a.az[i] = a.G * (sz0 + sz1);
+      if (COUNT && a.counts) a.counts[i] = cnt_lane;
+    }
+    if (COUNT && a.inter_total) {
+      unsigned long long c = owner ? (unsigned long long)cnt_lane : 0ull;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(full, c, o);
+      if (lane == 0) atomicAdd(a.inter_total, c);
+    }
+  }
+}
+
+template <bool COUNT, bool ZERO_EPS>
+static int group_walk_occupancy() {
+  static const int occ = [] {
+    int b = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bh_group_walk_kernel<COUNT, ZERO_EPS>, 256,
+                                                  0);
+    return std::max(b, 1);
+  }();
+  return occ;
+}
+
+template <bool COUNT, bool ZERO_EPS>
+static void launch_group_walk(const GroupWalkArgs& g, int64_t n, cudaStream_t st) {
+  // persistent warps: one resident wave, never more warps than bodies
+  const int64_t blocks = std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(n, 8), (int64_t)num_sms() * group_walk_occupancy<COUNT, ZERO_EPS>()));
+  bh_group_walk_kernel<COUNT, ZERO_EPS><<<(unsigned)blocks, 256, 0, st>>>(g);
+}
+
+// Shared stack entries the group walk uses before spilling to global memory
+// (a test hook: lowering it exercises the spill path on small inputs).
+static std::atomic<int> g_group_stack_limit{kGStack};
+
+void bh_set_group_stack_limit(int entries) { g_group_stack_limit.store(entries); }
+
+void bh_group_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, float* az,
+                          int32_t* counts, unsigned long long* inter_total, uint32_t* err,
+                          cudaStream_t st) {
+  const int64_t n = h.n;
+  if (!h.groups_ready)
+    fail(NBGB_ERR_INVALID_ARG, "Barnes-Hut group walk without groups from the tree build");
+  int4* groups = h.groups.ptr;
+  GroupCounters* gc = reinterpret_cast<GroupCounters*>(h.group_ctr.ptr);
+  int* ovf = grow(h.group_ovf, (size_t)kOvfChunks * kOvfChunk);
+  // the walk's task and overflow counters (the group count stays)
+  NBGB_CUDA(cudaMemsetAsync(&gc->task, 0, 2 * sizeof(uint32_t), st));
+  GroupWalkArgs g;
+  g.nodes = h.nodes.ptr;
+  g.spm = h.spm.ptr;
+  g.body = h.body;
+  g.nstart = h.nstart.ptr;
+  g.sv = SegView{h.seg_off_p, h.seg_base_p, h.seg_of.ptr, h.box.ptr};
+  g.groups = groups;
+  g.seg_root = h.seg_root.ptr;
+  g.n = n;
+  g.cap = h.cap;
+  g.theta2 = p.theta * p.theta;
+  g.eps2 = p.softening * p.softening;
+  g.G = p.G;
+  g.ax = ax;
+  g.ay = ay;
+  g.az = az;
+  g.counts = counts;
+  g.inter_total = inter_total;
+  g.gc = gc;
+  g.ovf = ovf;
+  g.err = err;
+  g.stack_limit = g_group_stack_limit.load();
+  const bool count = counts != nullptr || inter_total != nullptr;
+  const bool zero_eps = g.eps2 == 0.0f;
+  if (count) {
+    if (zero_eps)
+      launch_group_walk<true, true>(g, n, st);
+    else
+      launch_group_walk<true, false>(g, n, st);
+  } else {
+    if (zero_eps)
+      launch_group_walk<false, true>(g, n, st);
+    else
+      launch_group_walk<false, false>(g, n, st);
+  }
+  NBGB_LAUNCH_CHECK();
+}
+
+}  // namespace nbgb
