@@ -339,7 +339,9 @@ typedef struct nbgb_ensemble_stats {
   int64_t ticks;
   int64_t particle_steps;       /* sum over ticks of resident bodies */
   double direct_interactions;   /* sum of N (N - 1) over direct system-steps */
-  double bh_interactions;       /* interactions summed by the Barnes-Hut walks (device count) */
+  double bh_interactions;       /* interactions summed by the Barnes-Hut walks (device
+                                   count; group walk: list lengths minus one per body of
+                                   nonzero mass) */
   int64_t admitted;
   int64_t retired;
   int32_t resident;

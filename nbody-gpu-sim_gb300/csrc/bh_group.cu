@@ -92,8 +92,12 @@ __device__ __forceinline__ void group_eval(const float* ex, const float* ey, con
   }
 }
 
-template <bool COUNT, bool ZERO_EPS>
+// CNT: 0 no counting; 1 the total only (list lengths minus one per body of
+// nonzero mass, whose own leaf is in its list); 2 exact per-body counts (the
+// own leaf tracked as it is listed) and their total.
+template <int CNT, bool ZERO_EPS>
 __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) {
+  constexpr bool COUNT = CNT == 2;
   __shared__ int s_stack[8][kGStack];
   __shared__ __align__(16) float s_ring[8][4][kGRing];
   __shared__ __align__(16) float4 s_box[8][2];  // group box: centre, half sizes
@@ -310,8 +314,9 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
       a.az[i] = a.G * (sz0 + sz1);
       if (COUNT && a.counts) a.counts[i] = cnt_lane;
     }
-    if (COUNT && a.inter_total) {
-      unsigned long long c = owner ? (unsigned long long)cnt_lane : 0ull;
+    if (CNT > 0 && a.inter_total) {
+      const int own = CNT == 2 ? cnt_lane : (int)wr - (pi.w != 0.0f ? 1 : 0);
+      unsigned long long c = owner ? (unsigned long long)own : 0ull;
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(full, c, o);
       if (lane == 0) atomicAdd(a.inter_total, c);
@@ -319,23 +324,23 @@ __global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) 
   }
 }
 
-template <bool COUNT, bool ZERO_EPS>
+template <int CNT, bool ZERO_EPS>
 static int group_walk_occupancy() {
   static const int occ = [] {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bh_group_walk_kernel<COUNT, ZERO_EPS>, 256,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bh_group_walk_kernel<CNT, ZERO_EPS>, 256,
                                                   0);
     return std::max(b, 1);
   }();
   return occ;
 }
 
-template <bool COUNT, bool ZERO_EPS>
+template <int CNT, bool ZERO_EPS>
 static void launch_group_walk(const GroupWalkArgs& g, int64_t n, cudaStream_t st) {
   // persistent warps: one resident wave, never more warps than bodies
   const int64_t blocks = std::max<int64_t>(
-      1, std::min<int64_t>(ceil_div(n, 8), (int64_t)num_sms() * group_walk_occupancy<COUNT, ZERO_EPS>()));
-  bh_group_walk_kernel<COUNT, ZERO_EPS><<<(unsigned)blocks, 256, 0, st>>>(g);
+      1, std::min<int64_t>(ceil_div(n, 8), (int64_t)num_sms() * group_walk_occupancy<CNT, ZERO_EPS>()));
+  bh_group_walk_kernel<CNT, ZERO_EPS><<<(unsigned)blocks, 256, 0, st>>>(g);
 }
 
 // Shared stack entries the group walk uses before spilling to global memory
@@ -377,18 +382,23 @@ void bh_group_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, floa
   g.ovf = ovf;
   g.err = err;
   g.stack_limit = g_group_stack_limit.load();
-  const bool count = counts != nullptr || inter_total != nullptr;
+  const int cnt = counts ? 2 : (inter_total ? 1 : 0);
   const bool zero_eps = g.eps2 == 0.0f;
-  if (count) {
+  if (cnt == 2) {
     if (zero_eps)
-      launch_group_walk<true, true>(g, n, st);
+      launch_group_walk<2, true>(g, n, st);
     else
-      launch_group_walk<true, false>(g, n, st);
+      launch_group_walk<2, false>(g, n, st);
+  } else if (cnt == 1) {
+    if (zero_eps)
+      launch_group_walk<1, true>(g, n, st);
+    else
+      launch_group_walk<1, false>(g, n, st);
   } else {
     if (zero_eps)
-      launch_group_walk<false, true>(g, n, st);
+      launch_group_walk<0, true>(g, n, st);
     else
-      launch_group_walk<false, false>(g, n, st);
+      launch_group_walk<0, false>(g, n, st);
   }
   NBGB_LAUNCH_CHECK();
 }
