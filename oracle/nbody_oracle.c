@@ -695,7 +695,7 @@ int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const f
     /* interaction list */
     int cap = 4096, len = 0, own[ORC_GROUP] = {0};
     float* list = (float*)malloc(sizeof(float) * 4 * (size_t)cap);
-    int* stk = (int*)malloc(sizeof(int) * (size_t)(num_nodes + 8));
+    int stk[512]; /* depth-first: at most 7 pending siblings per level, depth <= 32 */
     int s = 0;
     stk[s++] = 0;
     while (s > 0) {
@@ -716,9 +716,14 @@ int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const f
         float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
         float size2 = 4.0f * nd->half * nd->half;
         entry = !overlap && size2 < theta2 * d2;
-        if (!entry)
+        if (!entry) {
+          if (s + 8 > 512) {
+            bad = 1;
+            continue;
+          }
           for (int c = 7; c >= 0; c--)
             if (nd->children[c] >= 0) stk[s++] = nd->children[c];
+        }
       }
       if (entry) {
         if (len == cap) {
@@ -751,7 +756,6 @@ int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const f
       if (interactions) interactions[i] = len - own[j];
     }
     free(list);
-    free(stk);
   }
   free(groups);
   return bad ? ORC_ERR_ARG : ORC_OK;

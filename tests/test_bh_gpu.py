@@ -334,8 +334,13 @@ def test_full_size_two_plummer(nb, orc):
     np.testing.assert_array_equal(r8["inter"][t], oint)
     err8 = vec_rel_err(*(a[t] for a in r8["acc"]), bx, by, bz)
     assert np.median(err8) <= 2e-3
-    # and with the group walk: lower error than the reference walk
-    rg = _bh(nb, s, theta=0.5, count=False, group=True)
+    # and with the group walk: every body's list length equals the oracle's
+    # group walk on the same tree, forces within 1e-5 of it, and a lower
+    # error against FP64 than the reference walk
+    rg = _bh(nb, s, theta=0.5, group=True)
+    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.5, 1.0, 0.01)
+    np.testing.assert_array_equal(rg["inter"], oint)
+    assert np.percentile(vec_rel_err(*rg["acc"], ox, oy, oz), 99) <= 1e-5
     errg = vec_rel_err(*(a[t] for a in rg["acc"]), bx, by, bz)
     assert np.median(errg) <= np.median(err)
 
