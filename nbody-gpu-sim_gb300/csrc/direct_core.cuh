@@ -76,7 +76,7 @@ __device__ __forceinline__ bool direct_tiles(TileRing& ring, const float4* __res
           ax2[p] = ay2[p] = az2[p] = f2_make(0.f, 0.f);
         }
         const f2 e2 = f2_make(eps2, eps2);
-#pragma unroll 4
+#pragma unroll 32
         for (int k = 0; k < kDirTile; ++k) {
           const float4 pj = tile[k];
           const f2 xj = f2_make(pj.x, pj.x), yj = f2_make(pj.y, pj.y), zj = f2_make(pj.z, pj.z);
