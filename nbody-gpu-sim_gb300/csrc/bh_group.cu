@@ -67,7 +67,7 @@ __device__ __forceinline__ void group_eval(const float* ex, const float* ey, con
   // FULL: one lane per body and a whole 32-entry chunk (fixed trip count);
   // entries are read as pairs straight into packed registers
   const int j0 = FULL ? 0 : 2 * r, jn = FULL ? 32 : cnt, js = FULL ? 2 : 2 * rep;
-#pragma unroll(FULL ? 4 : 1)
+#pragma unroll(FULL ? 16 : 1)
   for (int j = j0; j < jn; j += js) {
     const f2 xj{*reinterpret_cast<const unsigned long long*>(ex + base + j)};
     const f2 yj{*reinterpret_cast<const unsigned long long*>(ey + base + j)};
