@@ -314,8 +314,8 @@ def gpu_arm(args, rank, world, local):
         walk_share = (walk_ms / 1e3) / elapsed_s if elapsed_s > 0 else None
         direct_share = (dms / 1e3) / elapsed_s if elapsed_s > 0 else None
         # DRAM bytes of one group-walk launch: ncu capture at N = 1,048,576
-        # (two Plummer spheres, 192.4 MB read + written), scaled by the bodies
-        walk_traffic = 192.4e6 * bh_bodies / 1048576 if bh_bodies else None
+        # (two Plummer spheres, 188.6 MB read + written), scaled by the bodies
+        walk_traffic = 188.6e6 * bh_bodies / 1048576 if bh_bodies else None
         clocks = clk.summary()
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -371,8 +371,8 @@ def gpu_arm(args, rank, world, local):
                 "flops_per_interaction": 20, "share_of_tick": walk_share,
                 "walk_ms_per_tick": walk_ms / args.steps,
                 "note": "list evaluation in packed FP32x2 (6.3 FP32 instructions per "
-                        "entry) and a latency-bound traversal: FMA pipe 56 %, issue 67 %, "
-                        "shared-memory pipe 84 % (ncu, N=1M); interactions counted per "
+                        "entry) and a latency-bound traversal: FMA pipe 56 %, issue 65 %, "
+                        "shared-memory pipe 87 % (ncu, N=1M); interactions counted per "
                         "lane (list length minus the body itself)",
                 "hbm_peak_gbs_measured": measured_peaks().get("hbm_gbs"),
             },
