@@ -96,11 +96,11 @@ __device__ __forceinline__ void group_eval(const float* ex, const float* ey, con
 // nonzero mass, whose own leaf is in its list); 2 exact per-body counts (the
 // own leaf tracked as it is listed) and their total.
 template <int CNT, bool ZERO_EPS>
-__global__ void __launch_bounds__(256, 4) bh_group_walk_kernel(GroupWalkArgs a) {
+__global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kernel(GroupWalkArgs a) {
   constexpr bool COUNT = CNT == 2;
-  __shared__ int s_stack[8][kGStack];
-  __shared__ __align__(16) float s_ring[8][4][kGRing];
-  __shared__ __align__(16) float4 s_box[8][2];  // group box: centre, half sizes
+  __shared__ int s_stack[kGWarps][kGStack];
+  __shared__ __align__(16) float s_ring[kGWarps][4][kGRing];
+  __shared__ __align__(16) float4 s_box[kGWarps][2];  // group box: centre, half sizes
   const uint32_t total = a.nstart[a.n];
   if ((int64_t)total > a.cap) return;  // the tree build failed and said so
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -328,7 +328,7 @@ template <int CNT, bool ZERO_EPS>
 static int group_walk_occupancy() {
   static const int occ = [] {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bh_group_walk_kernel<CNT, ZERO_EPS>, 256,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bh_group_walk_kernel<CNT, ZERO_EPS>, kGWarps * 32,
                                                   0);
     return std::max(b, 1);
   }();
@@ -339,8 +339,9 @@ template <int CNT, bool ZERO_EPS>
 static void launch_group_walk(const GroupWalkArgs& g, int64_t n, cudaStream_t st) {
   // persistent warps: one resident wave, never more warps than bodies
   const int64_t blocks = std::max<int64_t>(
-      1, std::min<int64_t>(ceil_div(n, 8), (int64_t)num_sms() * group_walk_occupancy<CNT, ZERO_EPS>()));
-  bh_group_walk_kernel<CNT, ZERO_EPS><<<(unsigned)blocks, 256, 0, st>>>(g);
+      1, std::min<int64_t>(ceil_div(n, kGWarps),
+                           (int64_t)num_sms() * group_walk_occupancy<CNT, ZERO_EPS>()));
+  bh_group_walk_kernel<CNT, ZERO_EPS><<<(unsigned)blocks, kGWarps * 32, 0, st>>>(g);
 }
 
 // Shared stack entries the group walk uses before spilling to global memory

@@ -102,6 +102,7 @@ struct SegView {
 // Barnes-Hut group walk parameters (see the group walk below).
 constexpr int kGroupSize = 32;        // bodies per group (one per lane)
 constexpr int kGroupMergeMax = 1024;  // sibling subtrees merge only under parents this small
+constexpr int kGWarps = 8;            // warps (groups in flight) per block, 4 blocks per SM
 constexpr int kGStack = 512;          // per-warp shared stack (nodes to test)
 constexpr int kGRing = 64;            // per-warp ring of pending list entries
 constexpr int kOvfChunk = 8704;       // per-warp stack overflow: 32 x 8 siblings x 34 levels
