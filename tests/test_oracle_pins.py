@@ -218,3 +218,89 @@ def test_integrator_known_answers(orc):
     assert abs(z[0] - (0.5 - 0.2 * dt + 0.5 * 4.0 * dt * dt)) < 1e-6
     # :76-102 KE = 4.5
     assert abs(orc.kinetic_energy([1.0, 0.0], [0.0, 2.0], [0.0, 0.0], [1.0, 2.0]) - 4.5) < 1e-12
+
+
+def _py_group_walk(nodes, x, y, z, theta, eps):
+    """Restatement of the group walk in Python (float32 operations one at a
+    time; fma via an exact float64 product), pinning the C oracle's group
+    rule and acceptance arithmetic."""
+    f = np.float32
+    G, MERGE = 32, 1024
+
+    def bodies(ni):
+        nd = nodes[ni]
+        if nd["is_leaf"]:
+            return [int(nd["particle_index"])]
+        out = []
+        for c in nd["children"]:
+            if c >= 0:
+                out += bodies(int(c))
+        return out
+
+    groups = []
+    if nodes[0]["particle_count"] <= G:
+        groups.append([0])
+    stack = [] if nodes[0]["particle_count"] <= G else [0]
+    while stack:
+        nd = nodes[stack.pop()]
+        merge, gn = nd["particle_count"] <= MERGE, 0
+        for c in nd["children"]:
+            if c < 0:
+                continue
+            cc = int(nodes[c]["particle_count"])
+            if cc > G:
+                gn = 0
+                stack.append(int(c))
+            elif gn and merge and gn + cc <= G:
+                groups[-1].append(int(c))
+                gn += cc
+            else:
+                groups.append([int(c)])
+                gn = cc
+
+    def fma(a, b, c):
+        return f(np.float64(a) * np.float64(b) + np.float64(c))
+
+    th2, e2 = f(theta) * f(theta), f(eps) * f(eps)
+    counts = {}
+    for members in groups:
+        bs = [b for m in members for b in bodies(m)]
+        pos = [np.array([x[b], y[b], z[b]], np.float32) for b in bs]
+        lo, hi = np.min(pos, axis=0), np.max(pos, axis=0)
+        bc = (lo + hi) * f(0.5)
+        bh = np.maximum(hi - bc, bc - lo) * f(1.0 + 2.0 ** -22)
+        n_list, own = 0, set()
+        st = [0]
+        while st:
+            nd = nodes[st.pop()]
+            if nd["mass"] == 0:
+                continue
+            if nd["is_leaf"]:
+                n_list += 1
+                own.add(int(nd["particle_index"]))
+                continue
+            c, h, com = nd["center"], nd["half"], nd["com"]
+            overlap = all(abs(c[a] - bc[a]) <= h + bh[a] for a in range(3))
+            d = [max(abs(com[a] - bc[a]) - bh[a], f(0)) for a in range(3)]
+            d2 = fma(d[2], d[2], fma(d[1], d[1], fma(d[0], d[0], e2)))
+            size2 = f(4.0) * h * h
+            if not overlap and size2 < th2 * d2:
+                n_list += 1
+            else:
+                st += [int(ch) for ch in nd["children"][::-1] if ch >= 0]
+        for b in bs:
+            counts[b] = n_list - (1 if b in own else 0)
+    return np.array([counts[i] for i in range(len(x))])
+
+
+@pytest.mark.parametrize("n,theta", [(300, 0.5), (700, 0.3), (500, 1.0)])
+def test_group_walk_oracle_matches_python_restatement(orc, n, theta):
+    import nbgb.ics as ics
+    s = ics.plummer(n, seed=n)
+    x, y, z, m = (np.asarray(s[k], np.float32) for k in ("x", "y", "z", "m"))
+    bmin, bmax = orc.bbox(x, y, z)
+    _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
+    nodes, _, merges = orc.build_octree(x, y, z, m, si, bmin, bmax, max_nodes=64 * n + 64)
+    assert merges == 0
+    _, _, _, inter = orc.bh_group_forces(nodes, x, y, z, m, theta, 1.0, 0.01)
+    np.testing.assert_array_equal(inter, _py_group_walk(nodes, x, y, z, theta, 0.01))
