@@ -240,7 +240,9 @@ static void radix_sort_pairs_3phase(K* keys, K* keys_alt, uint32_t* vals, uint32
 // ------------------------------------------------- one-sweep radix sort --
 constexpr int kOSThreads = 256;
 constexpr int kOSItems = 16;
-constexpr int kOSTile = kOSThreads * kOSItems;  // == kSortTile
+constexpr int kOSTile = kOSThreads * kOSItems;
+// the workspace (radix_hist_elems) holds one status row per kSortTile keys
+static_assert(kOSTile == kSortTile, "one-sweep tile must match the workspace tile");
 constexpr int kOSWarps = kOSThreads / 32;
 constexpr int kOSWarpItems = kOSTile / kOSWarps;  // consecutive items per warp
 constexpr int kOSMaxPasses = 8;
