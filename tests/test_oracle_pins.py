@@ -220,10 +220,13 @@ def test_integrator_known_answers(orc):
     assert abs(orc.kinetic_energy([1.0, 0.0], [0.0, 2.0], [0.0, 0.0], [1.0, 2.0]) - 4.5) < 1e-12
 
 
-def _py_group_walk(nodes, x, y, z, theta, eps):
+def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False):
     """Restatement of the group walk in Python (float32 operations one at a
     time; fma via an exact float64 product), pinning the C oracle's group
-    rule and acceptance arithmetic."""
+    rule and acceptance arithmetic.  With check_reference_test, every cell
+    the group accepts is checked against the reference's per-target test
+    (force_barnes_hut.cu:218-224: not containing the body, 4h^2 / (d^2 +
+    eps^2) < theta^2) for every body of the group."""
     f = np.float32
     G, MERGE = 32, 1024
 
@@ -286,6 +289,13 @@ def _py_group_walk(nodes, x, y, z, theta, eps):
             size2 = f(4.0) * h * h
             if not overlap and size2 < th2 * d2:
                 n_list += 1
+                if check_reference_test:
+                    for b in bs:
+                        p = np.array([x[b], y[b], z[b]], np.float32)
+                        assert not all(abs(p[a] - c[a]) <= h for a in range(3))
+                        dd = com - p
+                        r2 = fma(dd[2], dd[2], fma(dd[1], dd[1], dd[0] * dd[0])) + e2
+                        assert size2 / r2 < th2
             else:
                 st += [int(ch) for ch in nd["children"][::-1] if ch >= 0]
         for b in bs:
@@ -303,4 +313,5 @@ def test_group_walk_oracle_matches_python_restatement(orc, n, theta):
     nodes, _, merges = orc.build_octree(x, y, z, m, si, bmin, bmax, max_nodes=64 * n + 64)
     assert merges == 0
     _, _, _, inter = orc.bh_group_forces(nodes, x, y, z, m, theta, 1.0, 0.01)
-    np.testing.assert_array_equal(inter, _py_group_walk(nodes, x, y, z, theta, 0.01))
+    np.testing.assert_array_equal(inter, _py_group_walk(nodes, x, y, z, theta, 0.01,
+                                                        check_reference_test=True))
