@@ -279,7 +279,47 @@ struct Retiring {
   nbgb_ensemble_result res;
   std::unique_ptr<ResidentSystem> sys;
   double* h_state = nullptr;  // pinned: 6n doubles + 3n floats (acc) + n floats (mass)
+  size_t h_bytes = 0;         // its capacity (a size class of the pinned pool)
   cudaEvent_t evt = nullptr;
+};
+
+// Pinned result buffers are recycled by size class (powers of two from
+// 64 KiB): page-locking host memory for every finished request costs about a
+// millisecond per megabyte, and cudaFreeHost waits for the device, which
+// would drain the tick pipeline at every retirement.
+constexpr size_t kPinnedMinBytes = size_t(64) << 10;
+constexpr size_t kPinnedPoolMaxBytes = size_t(256) << 20;  // idle buffers kept
+
+struct PinnedPool {
+  std::multimap<size_t, void*> idle;  // capacity -> buffer
+  size_t idle_bytes = 0;
+  void* take(size_t bytes, size_t* cap) {
+    size_t c = kPinnedMinBytes;
+    while (c < bytes) c <<= 1;
+    *cap = c;
+    auto it = idle.find(c);
+    if (it != idle.end()) {
+      void* p = it->second;
+      idle.erase(it);
+      idle_bytes -= c;
+      return p;
+    }
+    void* p = nullptr;
+    NBGB_CUDA(cudaMallocHost(&p, c));
+    return p;
+  }
+  void give(void* p, size_t cap) {
+    if (!p) return;
+    if (idle_bytes + cap > kPinnedPoolMaxBytes) {
+      cudaFreeHost(p);
+      return;
+    }
+    idle.emplace(cap, p);
+    idle_bytes += cap;
+  }
+  ~PinnedPool() {
+    for (auto& kv : idle) cudaFreeHost(kv.second);
+  }
 };
 
 }  // namespace nbgb
@@ -317,6 +357,7 @@ struct nbgb_ensemble {
   // staging for admissions
   DevBuf<float> stage;
   HostPinned<float> h_stage;
+  PinnedPool results;  // retirement read-back buffers
   // tables
   DevBuf<KDBlock> d_kd;
   DevBuf<SlotParams> d_slot;
@@ -602,7 +643,8 @@ static void retire(nbgb_ensemble* e, std::unique_ptr<ResidentSystem> s) {
   r.res.method = s->method;
   r.res.gpu_ms = 0.0;
   const size_t n = (size_t)s->n;
-  NBGB_CUDA(cudaMallocHost(&r.h_state, n * (6 * sizeof(double) + 4 * sizeof(float)) + 8));
+  r.h_state = static_cast<double*>(
+      e->results.take(n * (6 * sizeof(double) + 4 * sizeof(float)) + 8, &r.h_bytes));
   double* hd = r.h_state;
   DevBuf<double>* src[6] = {&e->x, &e->y, &e->z, &e->vx, &e->vy, &e->vz};
   for (int k = 0; k < 6; ++k)
@@ -971,7 +1013,7 @@ nbgb_status nbgb_ensemble_poll(nbgb_ensemble* e, nbgb_ensemble_result* result,
     if (h_out->mass) std::copy(f + 3 * n, f + 4 * n, h_out->mass);
   }
   if (state_f64) std::copy(r.h_state, r.h_state + 6 * n, state_f64);
-  cudaFreeHost(r.h_state);
+  e->results.give(r.h_state, r.h_bytes);
   cudaEventDestroy(r.evt);
   e->retiring.pop_front();
   if (bits) {

@@ -61,10 +61,10 @@ class Ensemble:
         cap = max(self.sizes.values()) if self.sizes else 0
         if want_state and cap:
             # large enough for whichever request finishes next
-            f64 = np.zeros(6 * cap, np.float64)
+            f64 = np.empty(6 * cap, np.float64)
         hout, facc = None, None
         if want_acc and cap:
-            facc = np.zeros((4, cap), np.float32)
+            facc = np.empty((4, cap), np.float32)
             hout = _lib.ParticleDataStruct()
             hout.acc_x, hout.acc_y, hout.acc_z, hout.mass = (facc[i].ctypes.data for i in range(4))
             hout.count = cap

@@ -133,6 +133,35 @@ def test_budget_and_resident_cap(nb):
     ens.close()
 
 
+def test_recycled_result_buffers(nb):
+    """Finished requests are read back through recycled pinned buffers: a
+    request that reuses the buffer of a larger one polled before it (same
+    size class) reads exactly its own state, equal to a run in a fresh
+    engine."""
+    from nbgb.serving import Ensemble
+    big, small = nb.ics.plummer(3000, seed=81), nb.ics.plummer(2500, seed=82)
+    ens = Ensemble(hbm_budget_bytes=1 << 30, direct_config=0)
+    got = []
+    for k, state in enumerate((big, small, big)):
+        rid = ens.submit(state, 7, 1e-3)
+        for _ in range(100):
+            ens.tick()
+            if ens.stats()["retired"] > k:
+                break
+        ens.synchronize()  # the read-back has landed
+        r = ens.poll(want_state=True, want_acc=True)
+        assert r is not None and r[0]["request_id"] == rid and r[0]["count"] == len(state["x"])
+        got.append(r[1])
+    ens.close()
+    fresh, _ = _run(nb, {"small": (small, 7)}, direct_config=0, hbm_budget_bytes=1 << 30)
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(got[1][k], fresh["small"][1][k])
+        np.testing.assert_array_equal(got[0][k], got[2][k])
+    for k in ("ax", "ay", "az", "m"):
+        np.testing.assert_array_equal(got[0][k], got[2][k])
+    np.testing.assert_array_equal(got[1]["m"], small["m"])
+
+
 def test_oversized_request_rejected(nb):
     from nbgb.serving import Ensemble
     ens = Ensemble(hbm_budget_bytes=1 << 20)
