@@ -371,7 +371,9 @@ nbgb_status nbgb_ensemble_tick(nbgb_ensemble* ens, int32_t* resident, int32_t* q
  * host arrays) is at least result->count, its non-NULL pos/vel/acc/mass
  * arrays receive the final FP32 state (acc = the acceleration at the final
  * positions); state_f64 (6*count doubles x, y, z, vx, vy, vz, or NULL) the
- * FP64 state. */
+ * FP64 state.  The engine reads results back into pinned host buffers that
+ * it recycles after the poll (at most 256 MiB kept idle, all freed by
+ * nbgb_ensemble_destroy); the caller's arrays may be pageable. */
 nbgb_status nbgb_ensemble_poll(nbgb_ensemble* ens, nbgb_ensemble_result* result,
                                nbgb_particle_data* h_out, double* state_f64);
 /* Wait for all retirements in flight. */
