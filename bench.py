@@ -65,10 +65,12 @@ def parse():
                     help="--impl reference: CPU seconds spread over warmup + steps")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--case", choices=["direct", "bh", "bh8", "bhg", "hash", "precision"], default=None,
+    ap.add_argument("--case", choices=["direct", "bh", "bh8", "bhg", "hash", "integrate",
+                                       "precision"], default=None,
                     help="time one plain force evaluation of a single system instead "
                          "(small profiling cases), or run the precision study")
-    ap.add_argument("--case-n", type=int, default=262144)
+    ap.add_argument("--case-n", type=int, default=None,
+                    help="bodies of a --case run (262144; 33554432 for integrate)")
     ap.add_argument("--precision-steps", type=int, default=2000)
     return ap.parse_args()
 
@@ -85,8 +87,9 @@ def precision_arm(args, local) -> dict:
     torch.cuda.set_device(local)
     eps, dt = 1e-3, 2.0 ** -10
     steps = args.precision_steps
-    out = {"case": "precision", "force_error": prec.force_errors(args.case_n, eps),
-           "energy_full_n": prec.energy_drift(args.case_n, eps, dt, steps,
+    n = args.case_n or 262144
+    out = {"case": "precision", "force_error": prec.force_errors(n, eps),
+           "energy_full_n": prec.energy_drift(n, eps, dt, steps,
                                               variants=("fp32", "fp32c_fp64")),
            "energy_small_n": prec.energy_drift(16384, eps, dt, steps)}
     return out
@@ -101,7 +104,7 @@ def case_arm(args, local):
 
     import nbgb
     torch.cuda.set_device(local)
-    n = args.case_n
+    n = args.case_n or 262144
     if args.case == "hash":
         side = 160.0 * (n / 4_194_304) ** (1.0 / 3.0)
         s = nbgb.ics.uniform_cube(n, seed=3, side=side)
@@ -129,6 +132,51 @@ def case_arm(args, local):
         torch.cuda.synchronize()
     calc.close()
     return {"case": args.case, "n": n, "ms_per_eval": e0.elapsed_time(e1) / args.steps}
+
+
+def integrate_arm(args, local):
+    """Achieved HBM bandwidth of the reference-semantics integrator kernels
+    (updatePositions, updateVelocities, storeOldAccelerations of
+    src/cuda/integrator.cu:12-49) through the public Integrator, on N bodies
+    whose arrays (52 B/body, 1.7 GB at the default N) exceed L2, so nothing is
+    flushed between launches.  Algorithmic bytes per body: positions 36 read
+    (pos, vel, acc) + 12 written; velocities 36 read (vel, acc_old, acc) + 12
+    written; store-old 12 read + 12 written.  Peak: the measured copy
+    bandwidth (read + write bytes) of MEASURED_PEAKS.json."""
+    import torch
+
+    import nbgb
+    torch.cuda.set_device(local)
+    n = args.case_n or (1 << 25)
+    rng = np.random.Generator(np.random.PCG64(9))
+    arrays = {k: rng.standard_normal(n, dtype=np.float32)
+              for k in ("pos_x", "pos_y", "pos_z", "vel_x", "vel_y", "vel_z",
+                        "acc_x", "acc_y", "acc_z")}
+    arrays["mass"] = np.full(n, 1.0 / n, np.float32)
+    peak = measured_peaks().get("hbm_gbs")
+    integ = nbgb.Integrator()
+    st = torch.cuda.current_stream()  # the legacy stream the Integrator launches on
+    out = {"case": "integrate", "n": n, "peak_gbs": peak,
+           "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy, read + write)"}
+    with nbgb.ScopedParticleData(n, arrays) as p:
+        kernels = (("vv_positions_kernel", lambda: integ.updatePositions(p.device, DT), 48),
+                   ("vv_velocities_kernel", lambda: integ.updateVelocities(p.device, DT), 48),
+                   ("store_old_kernel", lambda: integ.storeOldAccelerations(p.device), 24))
+        for name, fn, bpb in kernels:
+            for _ in range(max(args.warmup, 3)):
+                fn()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(args.steps):
+                fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            gbs = bpb * n / (ms / 1e3) / 1e9
+            out[name] = {"ms": ms, "bytes_per_body": bpb, "achieved_gbs": gbs,
+                         "frac": gbs / peak if peak else None}
+    return out
 
 
 def dist_env():
@@ -639,6 +687,8 @@ def main() -> int:
         dist.init_process_group("gloo")
     if args.case == "precision":
         out = precision_arm(args, local) if rank == 0 else None
+    elif args.case == "integrate":
+        out = integrate_arm(args, local) if rank == 0 else None
     elif args.case:
         out = case_arm(args, local) if rank == 0 else None
     elif args.impl == "reference":

@@ -14,6 +14,13 @@
 
 namespace nbgb {
 
+// The FP32 kernels take the reference's SoA struct, whose arrays the compiler
+// must assume may alias: each one issues all of a body's loads before its
+// first store, so the loads of the three components are in flight together
+// (with a load-store-load order per component the velocity update ran at
+// 72 % of the copy bandwidth instead of 96 %).  The arithmetic expressions are
+// the reference's.
+
 static inline unsigned grid_for(int64_t n, int threads) {
   int64_t b = std::min<int64_t>(ceil_div(std::max<int64_t>(n, 1), threads), (int64_t)num_sms() * 16);
   return (unsigned)std::max<int64_t>(b, 1);
@@ -26,19 +33,22 @@ __global__ void vv_positions_kernel(nbgb_particle_data d, float dt, bool store_o
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_pad;
        i += (int64_t)gridDim.x * blockDim.x) {
     if (i < n) {
-      float ax = d.acc_x[i], ay = d.acc_y[i], az = d.acc_z[i];
+      const float ax = d.acc_x[i], ay = d.acc_y[i], az = d.acc_z[i];
+      const float px = d.pos_x[i], py = d.pos_y[i], pz = d.pos_z[i];
+      const float vx = d.vel_x[i], vy = d.vel_y[i], vz = d.vel_z[i];
+      const float m = pack ? d.mass[i] : 0.f;
       if (store_old) {
         d.acc_old_x[i] = ax;
         d.acc_old_y[i] = ay;
         d.acc_old_z[i] = az;
       }
-      float x = d.pos_x[i] + fmaf(d.vel_x[i], dt, ax * dt2_half);
-      float y = d.pos_y[i] + fmaf(d.vel_y[i], dt, ay * dt2_half);
-      float z = d.pos_z[i] + fmaf(d.vel_z[i], dt, az * dt2_half);
+      const float x = px + fmaf(vx, dt, ax * dt2_half);
+      const float y = py + fmaf(vy, dt, ay * dt2_half);
+      const float z = pz + fmaf(vz, dt, az * dt2_half);
       d.pos_x[i] = x;
       d.pos_y[i] = y;
       d.pos_z[i] = z;
-      if (pack) pack[i] = make_float4(x, y, z, d.mass[i]);
+      if (pack) pack[i] = make_float4(x, y, z, m);
     } else if (pack) {
       pack[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
@@ -50,9 +60,12 @@ __global__ void vv_velocities_kernel(nbgb_particle_data d, float dt) {
   const float dt_half = 0.5f * dt;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    d.vel_x[i] += (d.acc_old_x[i] + d.acc_x[i]) * dt_half;
-    d.vel_y[i] += (d.acc_old_y[i] + d.acc_y[i]) * dt_half;
-    d.vel_z[i] += (d.acc_old_z[i] + d.acc_z[i]) * dt_half;
+    const float vx = d.vel_x[i], vy = d.vel_y[i], vz = d.vel_z[i];
+    const float ox = d.acc_old_x[i], oy = d.acc_old_y[i], oz = d.acc_old_z[i];
+    const float ax = d.acc_x[i], ay = d.acc_y[i], az = d.acc_z[i];
+    d.vel_x[i] = vx + (ox + ax) * dt_half;
+    d.vel_y[i] = vy + (oy + ay) * dt_half;
+    d.vel_z[i] = vz + (oz + az) * dt_half;
   }
 }
 
@@ -60,9 +73,10 @@ __global__ void store_old_kernel(nbgb_particle_data d) {
   const int64_t n = (int64_t)d.count;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
-    d.acc_old_x[i] = d.acc_x[i];
-    d.acc_old_y[i] = d.acc_y[i];
-    d.acc_old_z[i] = d.acc_z[i];
+    const float ax = d.acc_x[i], ay = d.acc_y[i], az = d.acc_z[i];
+    d.acc_old_x[i] = ax;
+    d.acc_old_y[i] = ay;
+    d.acc_old_z[i] = az;
   }
 }
 

@@ -43,6 +43,48 @@ def test_constant_acceleration_kinematics(nb):
         assert abs(h["pos_z"][0] - (0.5 - 0.2 * dt + 0.5 * 4.0 * dt * dt)) < 1e-6
 
 
+def _fma32(a, b, c):
+    # float32 fused multiply-add: the product of two floats is exact in
+    # float64; the float64 sum then rounds to float32 (a double rounding that
+    # differs from one rounding with probability ~2^-29 per element)
+    return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(np.float32)
+
+
+def test_fp32_kernels_bitwise_ragged(nb):
+    """storeOldAccelerations, updatePositions and updateVelocities on a
+    ragged N against the reference formulas (integrator.cu:12-49) in float32
+    with the device's rounding: x + fma(v, dt, a * (0.5 dt dt)) and
+    v + (a_old + a) * (0.5 dt) with the final multiply-add fused.  acc_old is
+    set on the device by storeOldAccelerations (the host copies carry pos,
+    vel, acc and mass only, as the reference's).  Bit-exact."""
+    n = (1 << 20) + 3
+    rng = np.random.Generator(np.random.PCG64(17))
+    keys = ("pos_x", "pos_y", "pos_z", "vel_x", "vel_y", "vel_z", "acc_x", "acc_y", "acc_z")
+    arr = {k: rng.standard_normal(n, dtype=np.float32) for k in keys}
+    arr["mass"] = rng.uniform(0.5, 1.5, n).astype(np.float32)
+    new_acc = {c: rng.standard_normal(n, dtype=np.float32) for c in "xyz"}
+    dt = np.float32(1e-2)
+    integ = nb.Integrator()
+    with nb.ScopedParticleData(n, arr) as p:
+        integ.storeOldAccelerations(p.device)  # acc_old = the uploaded acc
+        for c in "xyz":
+            p.host["acc_" + c][:] = new_acc[c]
+        p.upload()  # pos, vel, acc, mass; acc_old stays on the device
+        integ.updatePositions(p.device, float(dt))
+        integ.updateVelocities(p.device, float(dt))
+        p.download()
+        got = {k: p.host[k].copy() for k in keys}
+    h2 = np.float32(np.float32(0.5) * dt) * dt
+    hv = np.float32(0.5) * dt
+    for c in "xyz":
+        a, o = new_acc[c], arr["acc_" + c]
+        want_x = arr["pos_" + c] + _fma32(arr["vel_" + c], np.full(n, dt), a * h2)
+        np.testing.assert_array_equal(got["pos_" + c], want_x)
+        want_v = _fma32(o + a, np.full(n, hv), arr["vel_" + c])
+        np.testing.assert_array_equal(got["vel_" + c], want_v)
+        np.testing.assert_array_equal(got["acc_" + c], a)
+
+
 def test_kinetic_energy(nb):
     # :76-102
     arr = {"vel_x": np.array([1.0, 0.0], np.float32), "vel_y": np.array([0.0, 2.0], np.float32),
