@@ -7,8 +7,9 @@
  * pointers are `float*` in the caller's address space, streams are
  * `cudaStream_t` passed as `void*` (NULL = the library's own stream), and no
  * C++ exception crosses this boundary -- every call returns an nbgb_status
- * and leaves a message in nbgb_last_error().  A C++ adapter that rethrows the
- * reference's exception types is shown in INTEGRATION.md.
+ * and leaves a message in nbgb_last_error().  The C++ adapter in
+ * nbody-gpu-sim_gb300/adapter/nbody_adapter.cpp defines the reference's
+ * classes over this ABI and rethrows the reference's exception types.
  *
  * Threading: a calculator, system or ensemble handle must be used by one
  * host thread at a time (the reference's ParticleSystem is documented "Not
@@ -149,9 +150,14 @@ nbgb_status nbgb_compute_forces(nbgb_calculator* calc, const nbgb_particle_data*
  * calculator of the given G and softening: reads pos_x/y/z and mass, writes
  * acc_x/y/z (device pointers), compensated FP32 sums.  Limit: count <=
  * 65536 (larger counts return NBGB_ERR_INVALID_ARG).  Scratch is ~9 MiB of
- * static device memory per device, held from library load until exit; the
- * first call on a device resolves its address (make that first call before
- * any stream capture).  All calls share that scratch: calls that overlap on
+ * static device memory per device, held until exit.  With lazy module
+ * loading (the default of recent CUDA releases) the first call on a device
+ * reserves it and resolves its address, so that call may synchronise the
+ * device or fail with NBGB_ERR_OOM; a warm-up call with count 0 does exactly
+ * that and nothing else.  cudaDeviceReset after the first call on a device
+ * is not supported.  The call cannot run while `stream` is being captured
+ * (it returns NBGB_ERR_INVALID_ARG): it reads a device error word back and
+ * waits for the stream.  All calls share the scratch: calls that overlap on
  * the GPU race and must be serialised by the caller.  Work is enqueued on
  * `stream` (NULL = legacy default stream) and the call waits for it. */
 nbgb_status nbgb_compute_forces_direct_noalloc(const nbgb_particle_data* d_particles, float G,
@@ -415,6 +421,13 @@ nbgb_status nbgb_selftest_wait_timeout(uint32_t max_iters, uint32_t* error_bits)
  * the walk reports NBGB_ERR_OVERFLOW ("group walk stack overflow") at the
  * next synchronization instead of returning forces.  Process-wide. */
 nbgb_status nbgb_selftest_group_walk_stack(int32_t entries);
+
+/* Test hook for nbgb_compute_forces_direct_noalloc: the j-split count the
+ * regular direct planner picks for `count` bodies on the current device
+ * (*planned_splits) and the count the allocation-free entry point uses after
+ * capping it to its static partial-sum scratch (*used_splits, <= 8). */
+nbgb_status nbgb_selftest_noalloc_plan(int64_t count, int32_t* planned_splits,
+                                       int32_t* used_splits);
 
 /* ---------------------------------------------------------------------------
  * Library information.

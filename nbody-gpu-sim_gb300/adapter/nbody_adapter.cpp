@@ -6,7 +6,7 @@
 // src/cuda/force_direct.cu, force_barnes_hut.cu (calculator part),
 // force_spatial_hash.cu (calculator part) and integrator.cu, and links
 // libnbgb.so.  Everything above these classes (ParticleSystem, the app, the
-// benchmarks, the examples) is unchanged.  See INTEGRATION.md.
+// benchmarks, the examples) is unchanged.
 //
 // Mapping (reference declaration -> C ABI):
 //   ForceCalculator::computeForces      (force_calculator.hpp:12)  -> nbgb_compute_forces

@@ -7,18 +7,31 @@
 // synchronisation and its failure modes under memory pressure are
 // unacceptable.  The regular calculator (nbgb_compute_forces) keeps growable
 // per-calculator buffers and allocates them on first use; this entry point
-// instead uses scratch that lives in file-scope device arrays, reserved
-// once when the library is loaded on a device and held until the process
-// exits (about 9 MiB per device).
+// instead uses scratch that lives in file-scope device arrays (about 9 MiB
+// per device), held until the process exits.
 //
-// Limits: at most kNoAllocMaxBodies bodies per call, direct sum only.
-// All calls share the same scratch arrays: calls whose work overlaps on the
-// GPU (different streams, or different host threads, without ordering
-// between them) race on that scratch and must be serialised by the caller.
+// When the memory is reserved: the arrays belong to this library's device
+// module.  With eager module loading that happens when the library's module
+// is loaded on the device; with lazy loading (CUDA_MODULE_LOADING=LAZY, the
+// default of recent CUDA releases) it happens at the first call on that
+// device, which resolves the arrays' device addresses.  That first call can
+// therefore fail with NBGB_ERR_OOM under memory pressure or synchronise the
+// device; a warm-up call with count 0 does the reservation and nothing else.
+//
+// Limits: at most kNoAllocMaxBodies bodies per call, direct sum only; not
+// callable while its stream is being captured into a CUDA graph (it reads the
+// device error word back and waits for the stream); cudaDeviceReset after
+// the first call on a device is not supported (the resolved addresses are
+// kept per device).  All calls share the same scratch arrays: calls whose
+// work overlaps on the GPU (different streams, or different host threads,
+// without ordering between them) race on that scratch and must be
+// serialised by the caller.
 #include <mutex>
+#include <string>
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "runtime.cuh"
 
 namespace nbgb {
 
@@ -46,22 +59,53 @@ struct NoAllocScratch {
 static std::mutex g_noalloc_mu;
 static NoAllocScratch g_noalloc[64];
 
-static nbgb_status noalloc_scratch(int dev, NoAllocScratch* out) {
-  if (dev < 0 || dev >= 64) return NBGB_ERR_INVALID_ARG;
+static NoAllocScratch noalloc_scratch(int dev) {
+  if (dev < 0 || dev >= 64)
+    fail(NBGB_ERR_INVALID_ARG, "Validation Error: device ordinal beyond the no-allocation table");
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
   NoAllocScratch& s = g_noalloc[dev];
   if (!s.ready) {
-    if (cudaGetSymbolAddress(reinterpret_cast<void**>(&s.bodies), g_noalloc_bodies) != cudaSuccess ||
-        cudaGetSymbolAddress(reinterpret_cast<void**>(&s.partial), g_noalloc_partial) != cudaSuccess ||
-        cudaGetSymbolAddress(reinterpret_cast<void**>(&s.err), g_noalloc_err) != cudaSuccess) {
+    cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&s.bodies), g_noalloc_bodies);
+    if (e == cudaSuccess)
+      e = cudaGetSymbolAddress(reinterpret_cast<void**>(&s.partial), g_noalloc_partial);
+    if (e == cudaSuccess)
+      e = cudaGetSymbolAddress(reinterpret_cast<void**>(&s.err), g_noalloc_err);
+    if (e != cudaSuccess) {
       cudaGetLastError();
       s = NoAllocScratch{};
-      return NBGB_ERR_CUDA;
+      fail(e == cudaErrorMemoryAllocation ? NBGB_ERR_OOM : NBGB_ERR_CUDA,
+           std::string("CUDA Error: reserving the static no-allocation scratch: ") +
+               cudaGetErrorString(e));
     }
     s.ready = true;
   }
-  *out = s;
-  return NBGB_OK;
+  return s;
+}
+
+// The direct plan with its j-splits capped to the static partial-sum array.
+// `planned` receives the split count the regular planner chose.
+static DirectPlan noalloc_plan(int64_t n, int* planned) {
+  DirectPlan p = plan_direct(n, n, DirectVariant::kPaired8);
+  if (planned) *planned = p.splits;
+  if (p.splits > kNoAllocMaxSplits) {
+    p.tiles_per_split = ceil_div(p.n_tiles, kNoAllocMaxSplits);
+    p.splits = (int)ceil_div(p.n_tiles, p.tiles_per_split);
+  }
+  return p;
+}
+
+template <typename F>
+static nbgb_status noalloc_guarded(F&& f) {
+  try {
+    f();
+    return set_error(NBGB_OK, std::string());
+  } catch (const Error& e) {
+    return set_error(e.status, e.what());
+  } catch (const std::bad_alloc&) {
+    return set_error(NBGB_ERR_OOM, "host allocation failed");
+  } catch (const std::exception& e) {
+    return set_error(NBGB_ERR_CUDA, e.what());
+  }
 }
 
 }  // namespace nbgb
@@ -70,39 +114,65 @@ using namespace nbgb;
 
 extern "C" nbgb_status nbgb_compute_forces_direct_noalloc(const nbgb_particle_data* d, float G,
                                                           float softening, void* stream) {
-  try {
-    if (!d) return NBGB_ERR_INVALID_ARG;
-    if (!(std::isfinite(G) && G > 0.f) || !std::isfinite(softening) || softening < 0.f)
-      return NBGB_ERR_INVALID_ARG;
+  return noalloc_guarded([&] {
+    if (!d) fail(NBGB_ERR_INVALID_ARG, "Validation Error: null particle data");
+    if (!(std::isfinite(G) && G > 0.f))
+      fail(NBGB_ERR_INVALID_ARG,
+           "Validation Error: Gravitational constant must be positive and finite");
+    if (!std::isfinite(softening) || softening < 0.f)
+      fail(NBGB_ERR_INVALID_ARG,
+           "Validation Error: Softening parameter must be a finite, non-negative number");
     const int64_t n = (int64_t)d->count;
-    if (n > kNoAllocMaxBodies) return NBGB_ERR_INVALID_ARG;  // beyond the static scratch
-    if (n == 0) return NBGB_OK;
-    if (!d->pos_x || !d->pos_y || !d->pos_z || !d->mass || !d->acc_x || !d->acc_y || !d->acc_z)
-      return NBGB_ERR_INVALID_ARG;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return NBGB_ERR_NO_DEVICE;
-    NoAllocScratch s;
-    nbgb_status st = noalloc_scratch(dev, &s);  // first call on a device resolves the scratch
-    if (st != NBGB_OK) return st;
+    if (n > kNoAllocMaxBodies)
+      fail(NBGB_ERR_INVALID_ARG,
+           "Validation Error: the allocation-free direct sum takes at most 65536 bodies per call");
+    if (n > 0 &&
+        (!d->pos_x || !d->pos_y || !d->pos_z || !d->mass || !d->acc_x || !d->acc_y || !d->acc_z))
+      fail(NBGB_ERR_INVALID_ARG, "Validation Error: null position, mass or acceleration array");
     cudaStream_t cs = static_cast<cudaStream_t>(stream);
-    // The error word keeps the previous call's value: clear it first.
-    if (cudaMemsetAsync(s.err, 0, sizeof(uint32_t), cs) != cudaSuccess) return NBGB_ERR_CUDA;
-    DirectPlan p = plan_direct(n, n, DirectVariant::kPaired8);
-    if (p.splits > kNoAllocMaxSplits) {
-      p.tiles_per_split = ceil_div(p.n_tiles, kNoAllocMaxSplits);
-      p.splits = (int)ceil_div(p.n_tiles, p.tiles_per_split);
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    NBGB_CUDA(cudaStreamIsCapturing(cs, &cap));
+    if (cap != cudaStreamCaptureStatusNone)
+      fail(NBGB_ERR_INVALID_ARG,
+           "Validation Error: the allocation-free direct sum cannot run while its stream is "
+           "being captured");
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+      cudaGetLastError();
+      fail(NBGB_ERR_NO_DEVICE, "CUDA Error: no CUDA device");
     }
+    // the first call on a device resolves (and, with lazy module loading,
+    // reserves) the scratch; a count of 0 stops right after that
+    const NoAllocScratch s = noalloc_scratch(dev);
+    if (n == 0) return;
+    // The error word keeps the previous call's value: clear it first.
+    NBGB_CUDA(cudaMemsetAsync(s.err, 0, sizeof(uint32_t), cs));
+    const DirectPlan p = noalloc_plan(n, nullptr);
     // Every padded body slot and every partial read below is rewritten by
     // this call, so nothing else of the previous call's contents is used.
     launch_pack_soa(d->pos_x, d->pos_y, d->pos_z, d->mass, n, p.n_src_pad, s.bodies, cs);
     launch_direct(p, s.bodies, s.bodies, n, G, softening * softening, true, s.partial, d->acc_x,
                   d->acc_y, d->acc_z, s.err, cs);
     uint32_t bits = 0;
-    if (cudaMemcpyAsync(&bits, s.err, sizeof bits, cudaMemcpyDeviceToHost, cs) != cudaSuccess)
-      return NBGB_ERR_CUDA;
-    if (cudaStreamSynchronize(cs) != cudaSuccess) return NBGB_ERR_CUDA;
-    return bits ? NBGB_ERR_DEVICE_TIMEOUT : NBGB_OK;
-  } catch (const Error& e) {
-    return e.status;
-  }
+    NBGB_CUDA(cudaMemcpyAsync(&bits, s.err, sizeof bits, cudaMemcpyDeviceToHost, cs));
+    NBGB_CUDA(cudaStreamSynchronize(cs));
+    if (bits)
+      fail(NBGB_ERR_DEVICE_TIMEOUT,
+           "CUDA Error: a bounded device wait of the direct kernel ran out of iterations");
+  });
+}
+
+extern "C" nbgb_status nbgb_selftest_noalloc_plan(int64_t count, int32_t* planned_splits,
+                                                  int32_t* used_splits) {
+  return noalloc_guarded([&] {
+    if (count < 1 || count > kNoAllocMaxBodies)
+      fail(NBGB_ERR_INVALID_ARG, "Validation Error: count must be in [1, 65536]");
+    int planned = 0;
+    const DirectPlan p = noalloc_plan(count, &planned);
+    if ((int64_t)p.splits * p.n_tgt_pad > kNoAllocMaxSplits * kNoAllocMaxBodies ||
+        p.n_src_pad > kNoAllocMaxBodies)
+      fail(NBGB_ERR_OVERFLOW, "the capped plan does not fit the static scratch");
+    if (planned_splits) *planned_splits = planned;
+    if (used_splits) *used_splits = p.splits;
+  });
 }

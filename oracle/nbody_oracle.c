@@ -782,13 +782,23 @@ int orc_hash_dims(int64_t n, const float* x, const float* y, const float* z, flo
   return tot > 100000000 ? ORC_ERR_OVERFLOW : ORC_OK;
 }
 
-/* assignCellsKernel, force_spatial_hash.cu:29-50: floor((p-min)/cell) with
- * IEEE division, clamp to the grid, linear id x + y*gx + z*gx*gy. */
+/* Cell coordinates before the clamp: floor((p - min) / cell) per axis with
+ * IEEE division (assignCellsKernel, force_spatial_hash.cu:36-42; with
+ * min = 0 this is SpatialHashGrid::getCellIndex, :15-18). */
+void orc_cell_coords(float px, float py, float pz, const float bmin[3], float cell,
+                     int32_t out[3]) {
+  out[0] = (int32_t)floorf((px - bmin[0]) / cell);
+  out[1] = (int32_t)floorf((py - bmin[1]) / cell);
+  out[2] = (int32_t)floorf((pz - bmin[2]) / cell);
+}
+
+/* assignCellsKernel, force_spatial_hash.cu:29-50: the coordinates above,
+ * clamped to the grid, linear id x + y*gx + z*gx*gy. */
 static int32_t orc_cell_of(float px, float py, float pz, const float bmin[3], float cell,
                            const int dims[3]) {
-  int cx = (int)floorf((px - bmin[0]) / cell);
-  int cy = (int)floorf((py - bmin[1]) / cell);
-  int cz = (int)floorf((pz - bmin[2]) / cell);
+  int32_t c3[3];
+  orc_cell_coords(px, py, pz, bmin, cell, c3);
+  int cx = c3[0], cy = c3[1], cz = c3[2];
   cx = cx < 0 ? 0 : (cx > dims[0] - 1 ? dims[0] - 1 : cx);
   cy = cy < 0 ? 0 : (cy > dims[1] - 1 ? dims[1] - 1 : cy);
   cz = cz < 0 ? 0 : (cz > dims[2] - 1 ? dims[2] - 1 : cz);

@@ -76,6 +76,7 @@ class Oracle:
                                             _f32p, _f, _f, _f, _f32p, _f32p, _f32p, C.c_void_p]
         lib.orc_hash_dims.argtypes = [_i64, _f32p, _f32p, _f32p, _f, _f32p, _f32p, _i32p,
                                       C.POINTER(C.c_int64)]
+        lib.orc_cell_coords.argtypes = [_f, _f, _f, _f32p, _f, _i32p]
         lib.orc_hash_build.argtypes = [_i64, _f32p, _f32p, _f32p, _f, _f32p, _i32p, _i32p,
                                        _i32p, _i32p, _i32p]
         lib.orc_hash_forces.argtypes = [_i64, _f32p, _f32p, _f32p, _f32p, _f, _f32p, _i32p,
@@ -201,6 +202,23 @@ class Oracle:
         return ax, ay, az, inter
 
     # -- spatial hash ------------------------------------------------------------
+    def cell_coords(self, x, y, z, cell, bmin=(0.0, 0.0, 0.0)):
+        """Unclamped cell coordinates floor((p - bmin) / cell) of one point."""
+        out = np.zeros(3, np.int32)
+        self.lib.orc_cell_coords(x, y, z, _f32(bmin), cell, out)
+        return tuple(int(v) for v in out)
+
+    def hash_dims(self, x, y, z, cell):
+        """Padded box and grid dims of the hash grid; OverflowError above 1e8 cells."""
+        x, y, z = map(_f32, (x, y, z))
+        bmin, bmax = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        dims = np.zeros(3, np.int32)
+        tot = C.c_int64(0)
+        rc = self.lib.orc_hash_dims(len(x), x, y, z, cell, bmin, bmax, dims, C.byref(tot))
+        if rc != 0:
+            raise OverflowError("Spatial hash grid too large")
+        return dict(bmin=bmin, bmax=bmax, dims=dims, total_cells=tot.value)
+
     def hash_build(self, x, y, z, cell):
         x, y, z = map(_f32, (x, y, z))
         n = len(x)
@@ -250,6 +268,8 @@ class Reference:
         lib.ref_morton_code.argtypes = [_f, _f, _f]
         lib.ref_morton_code.restype = C.c_uint32
         lib.ref_cell_index.argtypes = [_f, _f, _f, _f, _i32p]
+        lib.ref_hash_grid_setup.argtypes = [_i64, _f32p, _f32p, _f32p, _f, _f32p, _f32p, _i32p,
+                                            C.POINTER(C.c_int64)]
         lib.ref_init_spherical.argtypes = [_i64, _f, _f, _f, _f, _f, _f, C.c_uint] + [_f32p] * 7
         lib.ref_init_uniform.argtypes = [_i64, _f32p, _f32p, _f, _f, C.c_uint] + [_f32p] * 7
         lib.ref_build_tree.argtypes = [_i64, _f32p, _f32p, _f32p, _f32p, _i32p, _f32p, _f32p,
@@ -272,6 +292,20 @@ class Reference:
         out = np.zeros(3, np.int32)
         self.lib.ref_cell_index(x, y, z, cell, out)
         return tuple(int(v) for v in out)
+
+    def hash_grid_setup(self, x, y, z, cell):
+        """The reference's padded box and grid dims (SpatialHashGrid::build up to
+        its first cell kernel); raises OverflowError where it rejects the grid."""
+        x, y, z = map(_f32, (x, y, z))
+        bmin, bmax = np.zeros(3, np.float32), np.zeros(3, np.float32)
+        dims = np.zeros(3, np.int32)
+        tot = C.c_int64(0)
+        rc = self.lib.ref_hash_grid_setup(len(x), x, y, z, cell, bmin, bmax, dims, C.byref(tot))
+        if rc == 2:
+            raise OverflowError("Spatial hash grid too large")
+        if rc != 0:
+            raise RuntimeError("reference grid setup did not stop at its first cell kernel")
+        return dict(bmin=bmin, bmax=bmax, dims=dims, total_cells=tot.value)
 
     def init_spherical(self, n, center=(0.0, 0.0, 0.0), radius=10.0, min_mass=1.0,
                        max_mass=1.0, seed=42):

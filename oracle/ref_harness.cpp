@@ -11,9 +11,10 @@
 // on the host from device copies (src/cuda/force_barnes_hut.cu:391-543).  To
 // run that host build without a GPU, this file supplies host-memory versions
 // of the four CUDA runtime memory calls the build uses (cudaMalloc, cudaFree,
-// cudaMemcpy, cudaMemset).  The shared object is linked with -Bsymbolic, so
-// the reference objects bind to these definitions and no device is touched.
-// No kernel of the reference is launched through this harness.
+// cudaMemcpy, cudaMemset), and intercepts kernel launches (see below).  The
+// shared object is linked with -Bsymbolic, so the reference objects bind to
+// these definitions and no device is touched.  No kernel of the reference
+// runs through this harness.
 
 #include <cstdint>
 #include <cstdlib>
@@ -37,6 +38,7 @@
 // specifiers do not change the ABI of the members.
 #define private public
 #include "nbody/barnes_hut_tree.hpp"
+#include "nbody/error_handling.hpp"
 #include "nbody/force_calculator.hpp"
 #include "nbody/particle_data.hpp"
 #include "nbody/serialization.hpp"
@@ -62,6 +64,71 @@ cudaError_t cudaMemset(void* dst, int value, size_t count) {
   if (count) std::memset(dst, value, count);
   return cudaSuccess;
 }
+}
+
+// ---- kernel launches ------------------------------------------------------
+// SpatialHashGrid::build (src/cuda/force_spatial_hash.cu:241-261) computes
+// its padded bounding box and grid dimensions on the host, between kernel
+// launches.  To run exactly that host code here, launches are intercepted:
+// the reference's bounding-box kernel (force_barnes_hut.cu:78-122, an exact
+// per-axis min/max) is replaced by the same min/max over the host arrays, and
+// every other launch is refused, so build() stops with its own CudaException
+// right after the dimensions are set (at the cell-assignment launch).
+namespace nbody {
+// host-side launch stub of the reference kernel (same symbol nvcc emits)
+void computeBoundingBoxKernel(const float* pos_x, const float* pos_y, const float* pos_z,
+                              float* min_x, float* min_y, float* min_z, float* max_x,
+                              float* max_y, float* max_z, int N);
+}  // namespace nbody
+
+static thread_local cudaError_t g_launch_error = cudaSuccess;
+
+extern "C" {
+// The launch sequence nvcc emits for `kernel<<<...>>>(args)`: push the
+// configuration, look the kernel handle up once, pop the configuration,
+// launch.  The handle is the host stub's address here.
+unsigned __cudaPushCallConfiguration(dim3, dim3, size_t, struct CUstream_st*) { return 0; }
+cudaError_t __cudaPopCallConfiguration(dim3* grid, dim3* block, size_t* shmem, void* stream) {
+  *grid = dim3(1, 1, 1);
+  *block = dim3(1, 1, 1);
+  *shmem = 0;
+  *static_cast<cudaStream_t*>(stream) = nullptr;
+  return cudaSuccess;
+}
+cudaError_t __cudaGetKernel(cudaKernel_t* kernel, const void* func) {
+  *kernel = reinterpret_cast<cudaKernel_t>(const_cast<void*>(func));
+  return cudaSuccess;
+}
+cudaError_t __cudaLaunchKernel(cudaKernel_t kernel, dim3, dim3, void** args, size_t,
+                               cudaStream_t) {
+  if (reinterpret_cast<const void*>(kernel) ==
+      reinterpret_cast<const void*>(&nbody::computeBoundingBoxKernel)) {
+    const float* p[3];
+    float* lo[3];
+    float* hi[3];
+    for (int a = 0; a < 3; ++a) {
+      p[a] = *static_cast<const float**>(args[a]);
+      lo[a] = *static_cast<float**>(args[3 + a]);
+      hi[a] = *static_cast<float**>(args[6 + a]);
+    }
+    const int n = *static_cast<int*>(args[9]);
+    for (int i = 0; i < n; ++i)
+      for (int a = 0; a < 3; ++a) {
+        *lo[a] = std::min(*lo[a], p[a][i]);
+        *hi[a] = std::max(*hi[a], p[a][i]);
+      }
+    return cudaSuccess;
+  }
+  g_launch_error = cudaErrorNotSupported;
+  return g_launch_error;
+}
+cudaError_t cudaGetLastError(void) {
+  const cudaError_t e = g_launch_error;
+  g_launch_error = cudaSuccess;
+  return e;
+}
+cudaError_t cudaPeekAtLastError(void) { return g_launch_error; }
+cudaError_t cudaDeviceSynchronize(void) { return cudaSuccess; }
 }
 
 static_assert(sizeof(nbody::OctreeNode) == 76, "OctreeNode layout");
@@ -158,6 +225,42 @@ int ref_build_tree(int64_t n, const float* x, const float* y, const float* z, co
   *max_depth = tree.getMaxDepth();
   if ((int64_t)*node_count > nodes_cap) return 1;
   std::memcpy(nodes_out, tree.getNodes(), (size_t)*node_count * sizeof(nbody::OctreeNode));
+  return 0;
+}
+
+// nbody::SpatialHashGrid::build up to its first cell kernel
+// (src/cuda/force_spatial_hash.cu:190-261): the reference's padded bounding
+// box (computeBoundingBox, :190-239) and grid dimensions (:249-252) for the
+// given positions and cell size.  Returns 0 with bmin/bmax/dims/total_cells
+// filled, 2 when the reference rejects the grid as too large (:257-260),
+// 1 on any other outcome.
+int ref_hash_grid_setup(int64_t n, const float* x, const float* y, const float* z, float cell,
+                        float bmin[3], float bmax[3], int dims[3], int64_t* total_cells) {
+  nbody::SpatialHashGrid grid((size_t)n, cell);
+  nbody::ParticleData pd;
+  pd.pos_x = const_cast<float*>(x);
+  pd.pos_y = const_cast<float*>(y);
+  pd.pos_z = const_cast<float*>(z);
+  pd.count = (size_t)n;
+  try {
+    grid.build(&pd);
+    return 1;  // cannot complete without a device: a launch must have been refused
+  } catch (const nbody::CudaException&) {
+    // stopped at the cell-assignment launch, after the dimensions were set
+  } catch (const std::runtime_error& e) {
+    if (std::string(e.what()).find("too large") != std::string::npos) return 2;
+    return 1;
+  }
+  bmin[0] = grid.bbox_min_.x;
+  bmin[1] = grid.bbox_min_.y;
+  bmin[2] = grid.bbox_min_.z;
+  bmax[0] = grid.bbox_max_.x;
+  bmax[1] = grid.bbox_max_.y;
+  bmax[2] = grid.bbox_max_.z;
+  dims[0] = grid.grid_dims_.x;
+  dims[1] = grid.grid_dims_.y;
+  dims[2] = grid.grid_dims_.z;
+  *total_cells = (int64_t)grid.total_cells_;
   return 0;
 }
 

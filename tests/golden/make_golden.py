@@ -14,6 +14,9 @@ oracle/_ref/libnbody_ref.so (ref_harness.cpp):
   * ref_pair.npz      -- computeGravitationalAccelerationCPU on seeded pairs;
   * ref_morton.npz    -- computeMortonCode on seeded and edge coordinates;
   * ref_cells.npz     -- SpatialHashGrid::getCellIndex on seeded points;
+  * ref_grids.npz     -- SpatialHashGrid::build's padded bounding box and
+                         grid dimensions (run on the host up to its first
+                         cell kernel) for seeded and edge point sets;
   * ref_trees.npz     -- BarnesHutTree::buildTreeOnHost node arrays for
                          several inputs (Morton-sorted with a stable sort);
   * ref_checkpoint.nbody -- Serializer::save of a small state.
@@ -84,6 +87,46 @@ def main() -> None:
     cells = np.concatenate([cells, np.array([2.0, 2.0, 2.0], np.float32)])
     ci = np.array([ref.cell_index(*pts[j], cells[j]) for j in range(len(pts))], np.int32)
     np.savez_compressed(os.path.join(HERE, "ref_cells.npz"), p=pts, cell=cells, idx=ci)
+
+    # --- hash grid setup: padded box and dims (SpatialHashGrid::build) ---------
+    grids = {}
+    gcases = []
+    for j, (lo, hi, n, cell) in enumerate([(0, 160, 3000, 2.0), (-50, 50, 3000, 3.7),
+                                          (-1e3, 1e3, 2000, 25.0), (0, 10, 1500, 0.5),
+                                          (-3, 7, 1000, 1.0), (1e4, 1e4 + 64, 1000, 2.0)]):
+        p = rng.uniform(lo, hi, (n, 3)).astype(np.float32)
+        gcases.append((f"u{j}", p, np.float32(cell)))
+    # edge sets: extents that are exact multiples of the cell, one point,
+    # coincident points, a flat slab, coordinates on cell boundaries
+    gcases.append(("grid_pts", np.stack(np.meshgrid(*[np.arange(0, 20, 2.0)] * 3),
+                                        -1).reshape(-1, 3).astype(np.float32), np.float32(2.0)))
+    gcases.append(("one", np.array([[1.5, -2.5, 3.0]], np.float32), np.float32(1.0)))
+    gcases.append(("coincident", np.full((64, 3), 4.0, np.float32), np.float32(0.25)))
+    slab = rng.uniform(-8, 8, (500, 3)).astype(np.float32)
+    slab[:, 2] = 0.5
+    gcases.append(("slab", slab, np.float32(0.8)))
+    names = []
+    for name, p, cell in gcases:
+        g = ref.hash_grid_setup(p[:, 0], p[:, 1], p[:, 2], cell)
+        grids[f"{name}_p"] = p
+        grids[f"{name}_cell"] = cell
+        grids[f"{name}_bmin"] = g["bmin"]
+        grids[f"{name}_bmax"] = g["bmax"]
+        grids[f"{name}_dims"] = g["dims"]
+        grids[f"{name}_total"] = np.int64(g["total_cells"])
+        names.append(name)
+    # a grid the reference rejects (more than 1e8 cells)
+    big = np.array([[0.0, 0.0, 0.0], [1000.0, 1000.0, 1000.0]], np.float32)
+    try:
+        ref.hash_grid_setup(big[:, 0], big[:, 1], big[:, 2], np.float32(2.0))
+        rejected = False
+    except OverflowError:
+        rejected = True
+    grids["too_large_p"] = big
+    grids["too_large_cell"] = np.float32(2.0)
+    grids["too_large_rejected"] = np.bool_(rejected)
+    grids["names"] = np.array(names)
+    np.savez_compressed(os.path.join(HERE, "ref_grids.npz"), **grids)
 
     # --- octrees built by the reference's host insertion -------------------
     trees = {}

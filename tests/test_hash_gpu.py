@@ -131,3 +131,19 @@ def test_full_size_uniform_cube(nb, orc):
     assert 30 < onb.mean() < 38  # ~34 neighbours within rc
     err = vec_rel_err(ax[t], ay[t], az[t], ox, oy, oz)
     assert np.percentile(err, 99) <= 1e-5
+
+
+def test_grid_setup_matches_reference_fixture(nb, golden):
+    # padded box and dims as the reference's own SpatialHashGrid::build host
+    # code computed them (tests/golden/ref_grids.npz, made by make_golden.py)
+    g = golden("ref_grids.npz")
+    for name in g["names"]:
+        p = g[f"{name}_p"]
+        cell = float(g[f"{name}_cell"])
+        s = {"x": p[:, 0].copy(), "y": p[:, 1].copy(), "z": p[:, 2].copy(),
+             "m": np.full(len(p), 1.0 / len(p), np.float32)}
+        _, cells, _ = _run(nb, s, cell, cell)
+        np.testing.assert_array_equal(cells["dims"], g[f"{name}_dims"], err_msg=name)
+        np.testing.assert_array_equal(cells["bmin"].view(np.uint32),
+                                      g[f"{name}_bmin"].view(np.uint32), err_msg=name)
+        assert cells["total_cells"] == int(g[f"{name}_total"]), name

@@ -38,13 +38,48 @@ def test_morton_codes_match_reference(orc, golden):
     np.testing.assert_array_equal(got, g["code"])
 
 
-def test_cell_index_known_answer(golden):
-    # tests/test_spatial_hash.cpp:34-47; getCellIndex = floor(p / cell)
+def test_cell_index_known_answer(orc, golden):
+    # tests/test_spatial_hash.cpp:34-47: the oracle's cell coordinates with a
+    # zero origin are SpatialHashGrid::getCellIndex (force_spatial_hash.cu:15-18)
     g = golden("ref_cells.npz")
     p, c, idx = g["p"], g["cell"], g["idx"]
-    got = np.floor(p / c[:, None]).astype(np.int32)  # float32 IEEE division, as the kernel
+    got = np.array([orc.cell_coords(*p[j], c[j]) for j in range(len(p))], np.int32)
     np.testing.assert_array_equal(got, idx)
     assert tuple(idx[-2]) == (1, 2, 3)
+
+
+def test_cell_index_against_reference_code(orc):
+    # the same through the reference's compiled getCellIndex, where it exists
+    try:
+        from oracle.oracle import Reference
+        ref = Reference()
+    except (FileNotFoundError, OSError):
+        pytest.skip("reference sources not present")
+    rng = np.random.default_rng(11)
+    p = rng.uniform(-70, 70, (2000, 3)).astype(np.float32)
+    c = rng.choice(np.array([0.3, 1.0, 2.0, 5.5], np.float32), len(p))
+    for j in range(len(p)):
+        assert orc.cell_coords(*p[j], c[j]) == ref.cell_index(*p[j], c[j])
+
+
+def test_hash_grid_dims_match_reference(orc, golden):
+    # SpatialHashGrid::build's padded box (+-0.001, force_spatial_hash.cu:232-238)
+    # and dims = ceil(extent / cell) + 1 (:249-252), produced by the reference's
+    # own host code: the oracle reproduces every bit
+    g = golden("ref_grids.npz")
+    for name in g["names"]:
+        p = g[f"{name}_p"]
+        got = orc.hash_dims(p[:, 0], p[:, 1], p[:, 2], float(g[f"{name}_cell"]))
+        for k in ("bmin", "bmax"):
+            np.testing.assert_array_equal(got[k].view(np.uint32), g[f"{name}_{k}"].view(np.uint32),
+                                          err_msg=f"{name} {k}")
+        np.testing.assert_array_equal(got["dims"], g[f"{name}_dims"], err_msg=name)
+        assert got["total_cells"] == int(g[f"{name}_total"]), name
+    # the reference rejects grids above 1e8 cells (:257-260); so does the oracle
+    assert bool(g["too_large_rejected"])
+    p = g["too_large_p"]
+    with pytest.raises(OverflowError):
+        orc.hash_dims(p[:, 0], p[:, 1], p[:, 2], float(g["too_large_cell"]))
 
 
 def _tree_case(golden, name):
