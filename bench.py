@@ -65,7 +65,7 @@ def parse():
                     help="--impl reference: CPU seconds spread over warmup + steps")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
-    ap.add_argument("--case", choices=["direct", "bh", "bh8", "bhg", "hash", "integrate",
+    ap.add_argument("--case", choices=["direct", "bh", "bh8", "bhg", "bhg8", "hash", "integrate",
                                        "precision"], default=None,
                     help="time one plain force evaluation of a single system instead "
                          "(small profiling cases), or run the precision study")
@@ -97,7 +97,8 @@ def precision_arm(args, local) -> dict:
 
 def case_arm(args, local):
     """One system through nbgb_compute_forces: direct / Barnes-Hut (theta 0.5;
-    1 or 8 bodies per leaf, or the group walk) on a Plummer sphere, or the
+    1 or 8 bodies per leaf, with the reference-style walk or the group walk)
+    on a Plummer sphere, or the
     spatial hash on the uniform cube at the serving density; prints ms per
     evaluation."""
     import torch
@@ -114,8 +115,8 @@ def case_arm(args, local):
         calc = nbgb.DirectForceCalculator()
     else:
         s = nbgb.ics.two_plummer(n, seed=2)
-        calc = nbgb.BarnesHutCalculator(0.5, leaf_capacity=8 if args.case == "bh8" else 1,
-                                        group_walk=args.case == "bhg")
+        calc = nbgb.BarnesHutCalculator(0.5, leaf_capacity=8 if args.case in ("bh8", "bhg8") else 1,
+                                        group_walk=args.case in ("bhg", "bhg8"))
     calc.setSofteningParameter(EPS)
     st = torch.cuda.current_stream()
     calc.set_stream(st.cuda_stream)

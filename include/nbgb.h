@@ -85,7 +85,8 @@ typedef struct nbgb_params {
                              library chooses its own tiling */
   int32_t leaf_capacity;  /* Barnes-Hut bucket size: 1 = the reference tree and walk
                              (one body per leaf); 2..16 = subtrees with at most this
-                             many bodies are summed body by body when opened */
+                             many bodies are summed body by body when opened (both
+                             walks) */
   uint32_t flags;         /* NBGB_FLAG_* */
 } nbgb_params;
 
@@ -111,7 +112,9 @@ typedef struct nbgb_params {
  * cell's centre of mass to the box.  Every accepted cell passes the
  * reference's per-target test for every body of the group, so the force
  * error is at most that of the reference walk at the same theta; the
- * interaction sets differ from the reference's.  Needs leaf_capacity 1. */
+ * interaction sets differ from the reference's.  With leaf_capacity > 1 a
+ * node of at most that many bodies that is not accepted adds its bodies to
+ * the list instead of being opened (buckets). */
 #define NBGB_FLAG_GROUP_WALK 0x10u
 
 void nbgb_params_default(nbgb_params* p);
@@ -329,7 +332,7 @@ typedef struct nbgb_ensemble_config {
   int32_t use_graphs;        /* run the batched Barnes-Hut pass as a CUDA graph while the
                                 set of resident Barnes-Hut systems is unchanged */
   int32_t group_walk;        /* 1 (default) = Barnes-Hut group walk (NBGB_FLAG_GROUP_WALK);
-                                0 = the reference's per-target walk (leaf_capacity applies) */
+                                0 = the reference's per-target walk */
 } nbgb_ensemble_config;
 
 /* One finished request. */

@@ -64,8 +64,6 @@ static void validate_params(nbgb_method m, const nbgb_params& p) {
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: Barnes-Hut theta must be between 0 and 2");
     if (p.leaf_capacity < 1 || p.leaf_capacity > 16)
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: leaf capacity must be between 1 and 16");
-    if ((p.flags & NBGB_FLAG_GROUP_WALK) && p.leaf_capacity != 1)
-      fail(NBGB_ERR_INVALID_ARG, "Validation Error: the group walk needs leaf capacity 1");
   }
   if (m == NBGB_SPATIAL_HASH) {
     if (!(finite(p.cell_size) && p.cell_size > 0.f))

@@ -19,7 +19,9 @@ namespace nbgb {
 // from the cell's centre of mass to the box: every accepted cell passes the
 // reference's per-target test (force_barnes_hut.cu:218-224) for every body of
 // the group, so each target sees an equal or finer cell set than in the
-// reference walk.  Leaves contribute their bodies.  The list is evaluated by
+// reference walk.  Leaves contribute their bodies; with leaf_capacity > 1 a
+// node of at most that many bodies that is not accepted contributes its
+// bodies instead of being opened (buckets).  The list is evaluated by
 // all lanes at once, one target per lane (2 or 4 lanes per target in groups
 // of at most 16 or 8 bodies), in packed FP32x2 arithmetic.
 struct GroupWalkArgs {
@@ -44,6 +46,8 @@ struct GroupWalkArgs {
   int* ovf;                         // kOvfChunks x kOvfChunk stack overflow entries
   uint32_t* err;
   int stack_limit;                  // shared stack entries used (64 .. kGStack)
+  int leaf_cap;                     // > 1: an opened node of at most this many bodies adds
+                                    // its bodies (buckets) instead of its children
 };
 
 // Floats as unsigned integers with the same order (finite values).
@@ -212,7 +216,9 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
           const float dz = fmaxf(__fsub_rn(fabsf(__fsub_rn(cm.z, bc.z)), bh.z), 0.0f);
           const float d2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmaf_rn(dx, dx, a.eps2)));
           entry = !overlap && __int_as_float(w.y) < __fmul_rn(a.theta2, d2);
-          open = !entry;
+          // an opened bucket (at most leaf_cap bodies) lists its bodies
+          multi = !entry && cnt <= a.leaf_cap;
+          open = !entry && !multi;
         }
       }
       // next siblings below first children, so the walk goes depth first
@@ -244,8 +250,44 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
         rd += 32;
         __syncwarp();
       }
-      // multi-body (depth-32) leaves: their bodies one by one
-      unsigned bm = __ballot_sync(full, multi);
+      // bodies of small runs (opened buckets, small depth-32 leaves): every
+      // such lane appends body j of its run in round j
+      const bool small = multi && cnt <= kGSmallRun;
+      if (__any_sync(full, small)) {
+        const int left = small ? cnt : 0;
+        if (COUNT && small) {  // the group's bodies inside this run list themselves
+          const int lo = max(w.z, g.x), hi = min(w.z + cnt, g.x + g.y);
+          if (lo < hi) selfmask |= ((1u << (hi - lo)) - 1u) << (lo - g.x);
+        }
+        for (int j = 0;; ++j) {
+          const bool e = j < left;
+          const unsigned bj = __ballot_sync(full, e);
+          if (!bj) break;
+          if (e) {
+            const float4 q = a.spm[w.z + j];
+            const int slot = (int)((wr + __popc(bj & lt)) & (kGRing - 1));
+            ex[slot] = q.x;
+            ey[slot] = q.y;
+            ez[slot] = q.z;
+            em[slot] = q.w;
+          }
+          wr += __popc(bj);
+          __syncwarp();
+          if (wr - rd >= 32) {
+            if (rep == 1)
+              group_eval<ZERO_EPS, true>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, 0, 1, pi,
+                                         a.eps2, ax2, ay2, az2);
+            else
+              group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep,
+                                          pi, a.eps2, ax2, ay2, az2);
+            rd += 32;
+            __syncwarp();
+          }
+        }
+      }
+      // larger multi-body (depth-32) leaves: 32 bodies at a time, one leaf
+      // after the other
+      unsigned bm = __ballot_sync(full, multi && !small);
       while (bm) {
         const int src = __ffs(bm) - 1;
         bm &= bm - 1;
@@ -383,6 +425,7 @@ void bh_group_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, floa
   g.ovf = ovf;
   g.err = err;
   g.stack_limit = g_group_stack_limit.load();
+  g.leaf_cap = p.leaf_capacity;
   const int cnt = counts ? 2 : (inter_total ? 1 : 0);
   const bool zero_eps = g.eps2 == 0.0f;
   if (cnt == 2) {

@@ -105,6 +105,7 @@ constexpr int kGroupMergeMax = 1024;  // sibling subtrees merge only under paren
 constexpr int kGWarps = 8;            // warps (groups in flight) per block, 4 blocks per SM
 constexpr int kGStack = 512;          // per-warp shared stack (nodes to test)
 constexpr int kGRing = 64;            // per-warp ring of pending list entries
+constexpr int kGSmallRun = 16;        // bucket / leaf bodies listed lane-parallel up to this
 constexpr int kOvfChunk = 8704;       // per-warp stack overflow: 32 x 8 siblings x 34 levels
 constexpr int kOvfChunks = 256;       // overflow chunks per launch
 constexpr float kBoxWiden = 0x1.000004p0f;  // 1 + 2^-22: covers the half sizes' rounding

@@ -878,8 +878,6 @@ nbgb_status nbgb_ensemble_create(const nbgb_ensemble_config* cfg, nbgb_ensemble*
     if (c.direct_config >= kNumConfigs) fail(NBGB_ERR_INVALID_ARG, "Validation Error: unknown direct configuration");
     if (c.leaf_capacity < 1 || c.leaf_capacity > 16)
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: leaf capacity must be between 1 and 16");
-    if (c.group_walk && c.leaf_capacity != 1)
-      fail(NBGB_ERR_INVALID_ARG, "Validation Error: the group walk needs leaf capacity 1");
     if (c.max_resident < 1 || c.hbm_budget_bytes < (1u << 20))
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: budget or resident cap too small");
     auto e = std::make_unique<nbgb_ensemble>();

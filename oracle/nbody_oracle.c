@@ -604,7 +604,9 @@ int orc_bh_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* 
  * 4h^2 < theta^2 * fma(dz,dz, fma(dy,dy, fma(dx,dx, eps^2))), d the per-axis
  * distance max(|com - b| - half, 0) of the centre of mass outside the box;
  * otherwise its children are walked.  Every body of the group sums the whole list;
- * interactions per body = list length minus its own leaf.  With eps = 0 a
+ * interactions per body = list length minus its own leaf.  With leaf_cap > 1
+ * an internal node of at most leaf_cap bodies that is not accepted adds its
+ * bodies (in octant order) instead of its children.  With eps = 0 a
  * zero-distance entry adds nothing.  Multi-body (depth-32) leaves are not
  * supported here (their bodies are not listed in the node records):
  * returns ORC_ERR_ARG. */
@@ -616,10 +618,12 @@ typedef struct {
   int mem[8];
 } orc_group;
 
-static void orc_group_bodies(const orc_node* nodes, int ni, int* out, int* nb, int* bad) {
+/* Bodies of the subtree at ni in octant (path) order, at most cap. */
+static void orc_subtree_bodies(const orc_node* nodes, int ni, int* out, int* nb, int cap,
+                               int* bad) {
   const orc_node* nd = &nodes[ni];
   if (nd->is_leaf) {
-    if (nd->particle_count != 1 || *nb >= ORC_GROUP) {
+    if (nd->particle_count != 1 || *nb >= cap) {
       *bad = 1;
       return;
     }
@@ -627,12 +631,17 @@ static void orc_group_bodies(const orc_node* nodes, int ni, int* out, int* nb, i
     return;
   }
   for (int c = 0; c < 8; c++)
-    if (nd->children[c] >= 0) orc_group_bodies(nodes, nd->children[c], out, nb, bad);
+    if (nd->children[c] >= 0) orc_subtree_bodies(nodes, nd->children[c], out, nb, cap, bad);
+}
+
+static void orc_group_bodies(const orc_node* nodes, int ni, int* out, int* nb, int* bad) {
+  orc_subtree_bodies(nodes, ni, out, nb, ORC_GROUP, bad);
 }
 
 int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* x,
                         const float* y, const float* z, const float* m, float theta, float G,
-                        float eps, float* ax, float* ay, float* az, int32_t* interactions) {
+                        float eps, float* ax, float* ay, float* az, int32_t* interactions,
+                        int leaf_cap) {
   if (num_nodes < 1) return ORC_ERR_ARG;
   /* groups, by a pre-order pass over the nodes of more than ORC_GROUP bodies */
   orc_group* groups = (orc_group*)malloc(sizeof(orc_group) * (size_t)(n + 1));
@@ -716,6 +725,25 @@ int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const f
         float d2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, eps2)));
         float size2 = 4.0f * nd->half * nd->half;
         entry = !overlap && size2 < theta2 * d2;
+        if (!entry && leaf_cap > 1 && nd->particle_count <= leaf_cap) {
+          /* an opened bucket: its bodies join the list */
+          int bb[16], nbb = 0;
+          orc_subtree_bodies(nodes, (int)(nd - nodes), bb, &nbb, 16, &bad);
+          for (int q = 0; q < nbb; q++) {
+            if (len == cap) {
+              cap *= 2;
+              list = (float*)realloc(list, sizeof(float) * 4 * (size_t)cap);
+            }
+            list[4 * len] = x[bb[q]];
+            list[4 * len + 1] = y[bb[q]];
+            list[4 * len + 2] = z[bb[q]];
+            list[4 * len + 3] = m[bb[q]];
+            len++;
+            for (int j = 0; j < nb; j++)
+              if (body[j] == bb[q]) own[j] = 1;
+          }
+          continue;
+        }
         if (!entry) {
           if (s + 8 > 512) {
             bad = 1;

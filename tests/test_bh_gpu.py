@@ -231,9 +231,36 @@ def test_group_walk_overflow_is_reported(nb, small_group_stack):
     assert np.isfinite(r["acc"][0]).all()
 
 
-def test_group_walk_rejects_buckets(nb):
-    with pytest.raises(nb.ValidationException):
-        nb.BarnesHutCalculator(0.5, leaf_capacity=8, group_walk=True)
+@pytest.mark.parametrize("gen,n,theta,leaf", [("plummer", 5000, 0.5, 8), ("two", 50000, 0.5, 8),
+                                              ("cube", 30000, 0.5, 4), ("dense", 6000, 0.5, 16),
+                                              ("plummer", 3000, 1.0, 2), ("far", 6000, 0.3, 8)])
+def test_group_walk_buckets_match_oracle(nb, orc, gen, n, theta, leaf):
+    """Group walk over buckets (an opened node of at most `leaf` bodies lists
+    its bodies): per-body list lengths equal the oracle's bucket group walk on
+    the same tree, forces within 1e-5 of it (p99, vector relative)."""
+    s = _gen(nb, gen, n)
+    _, _, nodes, _, merges = _oracle_tree(orc, s)
+    assert merges == 0
+    r = _bh(nb, s, theta=theta, leaf=leaf, group=True)
+    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], theta, 1.0,
+                                           0.01, leaf)
+    np.testing.assert_array_equal(r["inter"], oint)
+    err = vec_rel_err(*r["acc"], ox, oy, oz)
+    assert np.percentile(err, 99) <= 1e-5, np.percentile(err, 99)
+
+
+def test_group_walk_buckets_with_coincident_bodies(nb, orc):
+    # small depth-32 leaves inside buckets and a large one (listed 32 at a time)
+    n = 4000
+    s = nb.ics.plummer(n, seed=31)
+    for k in ("x", "y", "z"):
+        s[k][100:105] = s[k][100]   # a 5-body depth-32 leaf
+        s[k][200:300] = s[k][200]   # a 100-body depth-32 leaf
+    bx, by, bz = orc.direct_f64(s["x"], s["y"], s["z"], s["m"], 1.0, 0.01)
+    for leaf in (1, 8):
+        r = _bh(nb, s, theta=0.0, leaf=leaf, group=True)
+        assert (r["inter"] == n - 1).all()
+        assert np.max(vec_rel_err(*r["acc"], bx, by, bz)) < 1e-4
 
 
 def test_small_theta_matches_direct(nb, golden):
@@ -343,4 +370,15 @@ def test_full_size_two_plummer(nb, orc):
     assert np.percentile(vec_rel_err(*rg["acc"], ox, oy, oz), 99) <= 1e-5
     errg = vec_rel_err(*(a[t] for a in rg["acc"]), bx, by, bz)
     assert np.median(errg) <= np.median(err)
+    # the workload as configured (leaf <= 8 bodies) on the group walk: list
+    # lengths equal the oracle's bucket group walk, forces within 1e-5 of it,
+    # median error <= 2e-3 and no worse than either reference-style walk
+    rg8 = _bh(nb, s, theta=0.5, leaf=8, group=True)
+    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.5, 1.0, 0.01,
+                                           8)
+    np.testing.assert_array_equal(rg8["inter"], oint)
+    assert np.percentile(vec_rel_err(*rg8["acc"], ox, oy, oz), 99) <= 1e-5
+    errg8 = vec_rel_err(*(a[t] for a in rg8["acc"]), bx, by, bz)
+    assert np.median(errg8) <= 2e-3
+    assert np.median(errg8) <= min(np.median(err), np.median(err8))
 

@@ -255,13 +255,15 @@ def test_integrator_known_answers(orc):
     assert abs(orc.kinetic_energy([1.0, 0.0], [0.0, 2.0], [0.0, 0.0], [1.0, 2.0]) - 4.5) < 1e-12
 
 
-def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False):
+def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False, leaf_cap=1):
     """Restatement of the group walk in Python (float32 operations one at a
     time; fma via an exact float64 product), pinning the C oracle's group
     rule and acceptance arithmetic.  With check_reference_test, every cell
     the group accepts is checked against the reference's per-target test
     (force_barnes_hut.cu:218-224: not containing the body, 4h^2 / (d^2 +
-    eps^2) < theta^2) for every body of the group."""
+    eps^2) < theta^2) for every body of the group.  With leaf_cap > 1 an
+    internal node of at most leaf_cap bodies that the group does not accept
+    lists its bodies instead of being opened."""
     f = np.float32
     G, MERGE = 32, 1024
 
@@ -310,7 +312,8 @@ def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False):
         n_list, own = 0, set()
         st = [0]
         while st:
-            nd = nodes[st.pop()]
+            ni = st.pop()
+            nd = nodes[ni]
             if nd["mass"] == 0:
                 continue
             if nd["is_leaf"]:
@@ -331,6 +334,10 @@ def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False):
                         dd = com - p
                         r2 = fma(dd[2], dd[2], fma(dd[1], dd[1], dd[0] * dd[0])) + e2
                         assert size2 / r2 < th2
+            elif leaf_cap > 1 and nd["particle_count"] <= leaf_cap:
+                bb = bodies(ni)  # an opened bucket lists its bodies
+                n_list += len(bb)
+                own.update(bb)
             else:
                 st += [int(ch) for ch in nd["children"][::-1] if ch >= 0]
         for b in bs:
@@ -338,8 +345,9 @@ def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False):
     return np.array([counts[i] for i in range(len(x))])
 
 
-@pytest.mark.parametrize("n,theta", [(300, 0.5), (700, 0.3), (500, 1.0)])
-def test_group_walk_oracle_matches_python_restatement(orc, n, theta):
+@pytest.mark.parametrize("n,theta,leaf", [(300, 0.5, 1), (700, 0.3, 1), (500, 1.0, 1),
+                                          (600, 0.5, 8), (400, 0.7, 4), (900, 0.5, 16)])
+def test_group_walk_oracle_matches_python_restatement(orc, n, theta, leaf):
     import nbgb.ics as ics
     s = ics.plummer(n, seed=n)
     x, y, z, m = (np.asarray(s[k], np.float32) for k in ("x", "y", "z", "m"))
@@ -347,6 +355,10 @@ def test_group_walk_oracle_matches_python_restatement(orc, n, theta):
     _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
     nodes, _, merges = orc.build_octree(x, y, z, m, si, bmin, bmax, max_nodes=64 * n + 64)
     assert merges == 0
-    _, _, _, inter = orc.bh_group_forces(nodes, x, y, z, m, theta, 1.0, 0.01)
+    _, _, _, inter = orc.bh_group_forces(nodes, x, y, z, m, theta, 1.0, 0.01, leaf)
     np.testing.assert_array_equal(inter, _py_group_walk(nodes, x, y, z, theta, 0.01,
-                                                        check_reference_test=True))
+                                                        check_reference_test=True,
+                                                        leaf_cap=leaf))
+    if leaf > 1:  # buckets only replace cells by finer entries: lists grow
+        _, _, _, inter1 = orc.bh_group_forces(nodes, x, y, z, m, theta, 1.0, 0.01, 1)
+        assert np.all(inter >= inter1)
