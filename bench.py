@@ -58,8 +58,9 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=20)
     ap.add_argument("--e2e-ticks", type=int, default=600,
                     help="ticks of the saturated end-to-end run")
-    ap.add_argument("--serve-requests", type=int, default=384)
-    ap.add_argument("--serve-max-s", type=float, default=120.0)
+    ap.add_argument("--serve-requests", type=int, default=4096,
+                    help="requests of the Poisson serving run (the workload's stream)")
+    ap.add_argument("--serve-max-s", type=float, default=900.0)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-budget-s", type=float, default=120.0,
                     help="--impl reference: CPU seconds spread over warmup + steps")
@@ -297,16 +298,18 @@ def gpu_arm(args, rank, world, local):
         dist.barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with Clocks(dev_index) as clk:
-        torch.cuda.nvtx.range_push("bench_timed")  # profilers can filter on this range
-        e0.record(est)
-        t_host = time.perf_counter()
-        for _ in range(args.steps):
-            ens.tick()
-        e1.record(est)
-        torch.cuda.synchronize()
-        host_s = time.perf_counter() - t_host
-        torch.cuda.nvtx.range_pop()
+    # clocks sampled every 100 ms over the timed ticks and the end-to-end run
+    # right after them (both under load)
+    clk = Clocks(dev_index).__enter__()
+    torch.cuda.nvtx.range_push("bench_timed")  # profilers can filter on this range
+    e0.record(est)
+    t_host = time.perf_counter()
+    for _ in range(args.steps):
+        ens.tick()
+    e1.record(est)
+    torch.cuda.synchronize()
+    host_s = time.perf_counter() - t_host
+    torch.cuda.nvtx.range_pop()
     elapsed_s = e0.elapsed_time(e1) / 1e3
     s1 = ens.stats()
     ps = s1["particle_steps"] - s0["particle_steps"]
@@ -320,6 +323,7 @@ def gpu_arm(args, rank, world, local):
     ens.close()
     # --- end to end at saturation: host arrays in, results read back ----------
     e2e_rep = e2e_arm(nbgb, Ensemble, backlog, states, S, tuned, args.e2e_ticks, world)
+    clk.__exit__(None, None, None)
     del states
 
     # --- reduction over ranks ---------------------------------------------------
@@ -360,6 +364,7 @@ def gpu_arm(args, rank, world, local):
                              h2d=h2d, d2h=d2h)
         # --- CPU baseline (reference CPU path, restated) -------------------------
         cpu = cpu_baseline(nbgb, stream, args.cpu_seconds)
+        cpu["direct_n1024_100_steps"] = c1_cpu_baseline(nbgb)
         force_err = measured_force_error(nbgb)
 
         ffma_peak = ffma.value
@@ -371,6 +376,7 @@ def gpu_arm(args, rank, world, local):
         # (two Plummer spheres, 188.6 MB read + written), scaled by the bodies
         walk_traffic = 188.6e6 * bh_bodies / 1048576 if bh_bodies else None
         clocks = clk.summary()
+        clocks["window"] = "timed ticks and the saturated end-to-end run"
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -419,9 +425,9 @@ def gpu_arm(args, rank, world, local):
                 "bound": "fp32", "achieved": w_achieved, "peak": ffma_peak, "unit": "TFLOP/s",
                 "frac": (w_achieved / ffma_peak) if w_achieved else None,
                 "traffic": walk_traffic,
-                "traffic_source": "ncu dram__bytes_read+write of one walk at N=1,048,576 "
-                                  "(profiles/bh_group_walk_two_plummer_1M.md), scaled by "
-                                  "bodies walked",
+                "traffic_source": "ncu dram__bytes_read+write of one group-walk launch at "
+                                  "N=1,048,576 (two Plummer spheres), scaled by the bodies "
+                                  "walked",
                 "algorithmic_bytes": 64 * 1.5 * bh_bodies + 28 * bh_bodies if bh_bodies else None,
                 "peak_source": "measured in-process: FFMA chains on every SM "
                                "(nbgb_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
@@ -437,12 +443,24 @@ def gpu_arm(args, rank, world, local):
                               "achieved_tflops": d_achieved, "share_of_tick": direct_share,
                               "note": "overlaps the Barnes-Hut chain on another stream"},
             "fp32_peaks": {"ffma_tflops": ffma.value, "ffma2_tflops": ffma2.value,
-                           "mufu_gops": mufu.value},
+                           "mufu_gops": mufu.value,
+                           "spec_tflops": spec_fp32_tflops(clocks.get("sm_max_mhz")),
+                           "spec_note": "SMs x 128 FP32 lanes x 2 flops x the maximum SM "
+                                        "clock (nvidia-smi)"},
             "cpu_baseline": cpu,
             "clocks": clocks,
             "gpu_launches": launches,
         }
     return out
+
+
+def spec_fp32_tflops(sm_max_mhz) -> float | None:
+    """Nominal FP32 FMA rate: SMs x 128 lanes x 2 flops x clock."""
+    if not sm_max_mhz:
+        return None
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    return sms * 128 * 2 * float(sm_max_mhz) * 1e6 / 1e12
 
 
 def measured_force_error(nbgb) -> dict:
@@ -574,26 +592,66 @@ def plain_arm(nbgb, reqs, steps) -> dict:
 
 def cpu_step(orc, nbgb, r) -> tuple[float, float]:
     """One Velocity-Verlet step of request r on the host through the
-    reference's CPU path as restated in oracle/ (pair-function direct sum in
-    reference order for N <= 8192; the reference insertion octree + walk for
-    the Barnes-Hut systems).  Returns (particle-steps, seconds)."""
+    reference's CPU path as restated in oracle/ (src/cuda/integrator.cu:12-37
+    update formulae around the forces: pair-function direct sum in reference
+    order for N <= 8192; the reference insertion octree + per-target walk for
+    the Barnes-Hut systems).  a(t) comes from a force evaluation before the
+    timer (direct) or is zero (Barnes-Hut: the update's cost does not depend
+    on its values).  Returns (particle-steps, seconds)."""
     s = make_state(nbgb, r)
     x, y, z, m = s["x"].copy(), s["y"].copy(), s["z"].copy(), s["m"]
     vx, vy, vz = s["vx"].copy(), s["vy"].copy(), s["vz"].copy()
-    if r["n"] <= 8192:
+    n = r["n"]
+    if n <= 8192:
         ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)  # a(t) of a running system
-        t0 = time.perf_counter()
-        ox, oy, oz = ax.copy(), ay.copy(), az.copy()
-        orc.update_positions(x, y, z, vx, vy, vz, ax, ay, az, DT)
-        ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
-        orc.update_velocities(vx, vy, vz, ox, oy, oz, ax, ay, az, DT)
-        return float(r["n"]), time.perf_counter() - t0
+
+        def forces():
+            return orc.direct_f32(x, y, z, m, 1.0, EPS)
+    else:
+        ax, ay, az = (np.zeros(n, np.float32) for _ in range(3))
+
+        def forces():
+            bmin, bmax = orc.bbox(x, y, z)
+            _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
+            nodes, _, _ = orc.build_octree(x, y, z, m, si, bmin, bmax)
+            return orc.bh_forces(nodes, x, y, z, m, 0.5, 1.0, EPS)[:3]
     t0 = time.perf_counter()
-    bmin, bmax = orc.bbox(x, y, z)
-    _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
-    nodes, _, _ = orc.build_octree(x, y, z, m, si, bmin, bmax)
-    orc.bh_forces(nodes, x, y, z, m, 0.5, 1.0, EPS)
-    return float(r["n"]), time.perf_counter() - t0
+    ox, oy, oz = ax.copy(), ay.copy(), az.copy()
+    orc.update_positions(x, y, z, vx, vy, vz, ax, ay, az, DT)
+    ax, ay, az = (np.ascontiguousarray(a, np.float32) for a in forces())
+    orc.update_velocities(vx, vy, vz, ox, oy, oz, ax, ay, az, DT)
+    return float(n), time.perf_counter() - t0
+
+
+def c1_cpu_baseline(nbgb) -> dict:
+    """The plain direct workload on the host: N = 1024 Plummer sphere, 100
+    Velocity-Verlet steps, eps = 0.01, dt = 1e-3, the reference's pair
+    function in its order (src/cuda/force_direct.cu:109-117) and update
+    formulae (src/cuda/integrator.cu:12-37), restated in oracle/; timed on one
+    core and on all host cores."""
+    from oracle.oracle import Oracle
+    orc = Oracle()
+    s = nbgb.ics.plummer(1024, seed=1)
+    all_threads = orc.num_threads()
+    out = {"workload": "Plummer N=1024, 100 Velocity-Verlet steps, eps=0.01, dt=1e-3",
+           "host_cores": os.cpu_count()}
+    for label, threads in (("one_core", 1), ("all_cores", all_threads)):
+        orc.set_num_threads(threads)
+        x, y, z, m = (s[k].copy() for k in ("x", "y", "z", "m"))
+        vx, vy, vz = (s[k].copy() for k in ("vx", "vy", "vz"))
+        ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
+        t0 = time.perf_counter()
+        for _ in range(100):
+            ox, oy, oz = ax, ay, az
+            orc.update_positions(x, y, z, vx, vy, vz, ax, ay, az, DT)
+            ax, ay, az = orc.direct_f32(x, y, z, m, 1.0, EPS)
+            orc.update_velocities(vx, vy, vz, ox, oy, oz, ax, ay, az, DT)
+        dt = time.perf_counter() - t0
+        out[label] = {"threads": threads, "seconds": dt, "ms_per_step": 10.0 * dt,
+                      "particle_steps_per_s": 1024 * 100 / dt,
+                      "interactions_per_s": 1024 * 1023 * 100 / dt}
+    orc.set_num_threads(all_threads)
+    return out
 
 
 def cpu_baseline(nbgb, stream, seconds) -> dict:

@@ -926,3 +926,12 @@ int orc_num_threads(void) {
   return 1;
 #endif
 }
+
+/* Threads of the OpenMP loops above (timing on one core vs all cores). */
+void orc_set_num_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}

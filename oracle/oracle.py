@@ -84,6 +84,7 @@ class Oracle:
                                         _i32p, _i32p, _i32p, _f, _f, _f, C.c_void_p, _i64,
                                         _f32p, _f32p, _f32p, C.c_void_p]
         lib.orc_num_threads.restype = C.c_int
+        lib.orc_set_num_threads.argtypes = [C.c_int]
         assert lib.orc_node_size() == 76
 
     # -- pair law / direct ---------------------------------------------------
@@ -255,6 +256,9 @@ class Oracle:
 
     def num_threads(self) -> int:
         return self.lib.orc_num_threads()
+
+    def set_num_threads(self, n: int) -> None:
+        self.lib.orc_set_num_threads(n)
 
 
 class Reference:
