@@ -185,6 +185,24 @@ nbgb_status nbgb_kinetic_energy(const nbgb_particle_data* d_particles, double* k
 nbgb_status nbgb_potential_energy(const nbgb_particle_data* d_particles, float G, float eps,
                                   double* pe, void* stream);
 
+/* FP64-state Velocity Verlet behind the reference's FP32 ParticleData, for
+ * ParticleSystem::update (src/core/particle_system.cpp:122-136) through
+ * Integrator::integrate (integrator.cu:175-189).  The library keeps x and v
+ * of each ParticleData (keyed by its pos_x device pointer) in FP64 across
+ * steps; one step is
+ *   nbgb_state_kick_drift:  acc_old = acc; v += acc dt/2 and x += v dt in
+ *                           FP64; pos = (float) x
+ *   (the caller's forces on pos -> acc)
+ *   nbgb_state_kick:        v += acc dt/2 in FP64; vel = (float) v
+ * -- the reference's update algebraically, with FP64 state.  After every
+ * step pos and vel are the rounded FP64 state.  An element whose FP32 value
+ * differs from its rounded FP64 value was changed by the caller and is taken
+ * over as the new state.  Enqueued on `stream` (NULL = legacy stream).
+ * nbgb_state_release frees a ParticleData's FP64 state (synchronises). */
+nbgb_status nbgb_state_kick_drift(const nbgb_particle_data* d_particles, float dt, void* stream);
+nbgb_status nbgb_state_kick(const nbgb_particle_data* d_particles, float dt, void* stream);
+nbgb_status nbgb_state_release(const nbgb_particle_data* d_particles);
+
 /* ---------------------------------------------------------------------------
  * ParticleDataManager (include/nbody/particle_data.hpp:9-28,
  * src/cuda/particle_init.cu:11-160): 13 separate device arrays, acc and

@@ -12,10 +12,14 @@
 //   ForceCalculator::computeForces      (force_calculator.hpp:12)  -> nbgb_compute_forces
 //   createForceCalculator               (force_calculator.hpp:76)  -> one adapter object per method
 //   computeGravitationalAccelerationCPU (force_calculator.hpp:79)  -> kept on the host
-//   Integrator::*                        (integrator.hpp:15-33)     -> nbgb_update_* / nbgb_*_energy
+//   Integrator::integrate                (integrator.hpp:19)        -> nbgb_state_kick_drift,
+//                                                                     computeForces, nbgb_state_kick
+//   Integrator::* (the other members)    (integrator.hpp:15-33)     -> nbgb_update_* / nbgb_*_energy
 // Status codes are rethrown as the reference's exception types
 // (include/nbody/error_handling.hpp).
+#include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <mutex>
@@ -307,16 +311,47 @@ void launchStoreAccelerationsKernel(ParticleData* d, int) {
   check(nbgb_store_old_accelerations(view(d), nullptr));
 }
 
+namespace {
+// ParticleData whose FP64 state an integrator keeps (released with it).
+std::unordered_map<const Integrator*, std::vector<ParticleData*>> g_integrated;
+
+// NBGB_FP32_VERLET=1: the reference's FP32 update kernels instead of the
+// FP64 state.
+bool fp32_verlet() {
+  const char* v = std::getenv("NBGB_FP32_VERLET");
+  return v && v[0] == '1';
+}
+}  // namespace
+
 Integrator::Integrator(int block_size) : block_size_(block_size) {}
-Integrator::~Integrator() = default;
+Integrator::~Integrator() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_integrated.find(this);
+  if (it == g_integrated.end()) return;
+  for (ParticleData* d : it->second) nbgb_state_release(view(d));
+  g_integrated.erase(it);
+}
 void Integrator::ensureScratchBuffer(size_t) {}  // reductions need no caller-visible scratch
 
+// Velocity Verlet (integrator.cu:175-189) with x and v kept in FP64 between
+// steps; the FP32 ParticleData is the rounded state after every step.
 void Integrator::integrate(ParticleData* d, ForceCalculator* force_calc, float dt) {
   NBODY_PROFILE_SCOPE("integrator.velocity_verlet");
-  storeOldAccelerations(d);
-  updatePositions(d, dt);
+  if (fp32_verlet()) {
+    storeOldAccelerations(d);
+    updatePositions(d, dt);
+    force_calc->computeForces(d);
+    updateVelocities(d, dt);
+    return;
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto& v = g_integrated[this];
+    if (std::find(v.begin(), v.end(), d) == v.end()) v.push_back(d);
+  }
+  check(nbgb_state_kick_drift(view(d), dt, nullptr));
   force_calc->computeForces(d);
-  updateVelocities(d, dt);
+  check(nbgb_state_kick(view(d), dt, nullptr));
 }
 void Integrator::updatePositions(ParticleData* d, float dt) {
   launchUpdatePositionsKernel(d, dt, block_size_);

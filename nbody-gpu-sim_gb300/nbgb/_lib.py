@@ -96,6 +96,9 @@ _SIGS = {
     "nbgb_calculator_synchronize": (C.c_int, [_vp]),
     "nbgb_compute_forces": (C.c_int, [_vp, _pd]),
     "nbgb_integrate": (C.c_int, [_vp, _pd, C.c_float]),
+    "nbgb_state_kick_drift": (C.c_int, [_pd, C.c_float, _vp]),
+    "nbgb_state_kick": (C.c_int, [_pd, C.c_float, _vp]),
+    "nbgb_state_release": (C.c_int, [_pd]),
     "nbgb_update_positions": (C.c_int, [_pd, C.c_float, _vp]),
     "nbgb_update_velocities": (C.c_int, [_pd, C.c_float, _vp]),
     "nbgb_store_old_accelerations": (C.c_int, [_pd, _vp]),

@@ -392,7 +392,18 @@ class Integrator:
         self.block_size = block_size
 
     def integrate(self, d: ParticleData, calc: ForceCalculator, dt: float) -> None:
+        """The reference's FP32 update kernels around the forces (integrator.cu:175-189)."""
         check(_lib.lib().nbgb_integrate(calc.handle, d.ptr(), dt))
+
+    def integrate_f64(self, d: ParticleData, calc: ForceCalculator, dt: float) -> None:
+        """The same step with x and v kept in FP64 by the library between steps
+        (the drop-in adapter's Integrator::integrate); d holds the rounded state."""
+        check(_lib.lib().nbgb_state_kick_drift(d.ptr(), dt, None))
+        calc.computeForces(d)
+        check(_lib.lib().nbgb_state_kick(d.ptr(), dt, None))
+
+    def release_state(self, d: ParticleData) -> None:
+        check(_lib.lib().nbgb_state_release(d.ptr()))
 
     def updatePositions(self, d: ParticleData, dt: float) -> None:  # noqa: N802
         check(_lib.lib().nbgb_update_positions(d.ptr(), dt, None))

@@ -237,3 +237,72 @@ def test_fp64_flag_requires_direct(nb):
     with pytest.raises(nb.ValidationException):
         nb.System(calc, s)
     calc.close()
+
+
+def test_state_mirror_trajectory_vs_fp64(nb, orc):
+    """The drop-in Integrator::integrate path (nbgb_state_kick_drift, the
+    calculator, nbgb_state_kick): x and v stay in FP64 inside the library
+    between steps.  The plain direct workload, 100 steps: the FP32 ParticleData
+    within 2e-5 (x) and 2e-4 (v) of the FP64 oracle's trajectory, and within
+    1e-6 of the device-resident system path (same FP32 forces, kicks merged
+    differently)."""
+    n, eps, dt, steps = _c1()
+    s = nb.ics.plummer(n, seed=1)
+    calc = nb.DirectForceCalculator()
+    calc.setSofteningParameter(eps)
+    integ = nb.Integrator()
+    arr = {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"], "vel_x": s["vx"],
+           "vel_y": s["vy"], "vel_z": s["vz"], "mass": s["m"]}
+    with nb.ScopedParticleData(n, arr) as p:
+        calc.computeForces(p.device)
+        for _ in range(steps):
+            integ.integrate_f64(p.device, calc, dt)
+        p.download()
+        got = {k: p.host[f].astype(np.float64) for k, f in
+               (("x", "pos_x"), ("y", "pos_y"), ("z", "pos_z"), ("vx", "vel_x"),
+                ("vy", "vel_y"), ("vz", "vel_z"))}
+        integ.release_state(p.device)
+    st = {k: s[k].astype(np.float64) for k in ("x", "y", "z", "vx", "vy", "vz")}
+    m = s["m"].astype(np.float64)
+    st["ax"], st["ay"], st["az"] = orc.direct_f64(st["x"], st["y"], st["z"], m, 1.0, eps)
+    for _ in range(steps):
+        orc.vv_step_f64(st, m, 1.0, eps, float(np.float32(dt)))
+    assert max(np.abs(got[k] - st[k]).max() for k in ("x", "y", "z")) <= 2e-5
+    assert max(np.abs(got[k] - st[k]).max() for k in ("vx", "vy", "vz")) <= 2e-4
+    sysm = nb.System(calc, s)
+    sysm.step(dt, steps)
+    ref = sysm.read_f64()
+    sysm.close()
+    calc.close()
+    assert max(np.abs(got[k] - ref[k]).max() for k in ("x", "y", "z", "vx", "vy", "vz")) <= 1e-6
+
+
+def test_state_mirror_takes_caller_changes(nb):
+    """A value the caller writes into the FP32 ParticleData between steps (a
+    reset, a checkpoint load) becomes the state: the next step starts from it."""
+    n, eps, dt = 2000, 0.01, 1e-3
+    s = nb.ics.plummer(n, seed=5)
+    calc = nb.DirectForceCalculator()
+    calc.setSofteningParameter(eps)
+    integ = nb.Integrator()
+    arr = {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"], "vel_x": s["vx"],
+           "vel_y": s["vy"], "vel_z": s["vz"], "mass": s["m"]}
+    with nb.ScopedParticleData(n, arr) as p:
+        calc.computeForces(p.device)
+        for _ in range(5):
+            integ.integrate_f64(p.device, calc, dt)
+        p.download()
+        p.host["pos_x"][7] += np.float32(0.5)
+        p.host["vel_y"][3] = np.float32(0.25)
+        p.upload()
+        x0, v0 = float(p.host["pos_x"][7]), float(p.host["vel_x"][7])
+        a0 = float(p.host["acc_x"][7])
+        vy0, ay0 = float(p.host["vel_y"][3]), float(p.host["acc_y"][3])
+        integ.integrate_f64(p.device, calc, dt)
+        p.download()
+        assert abs(p.host["pos_x"][7] - (x0 + v0 * dt + 0.5 * a0 * dt * dt)) <= 1e-6
+        ay1 = float(p.host["acc_y"][3])
+        assert abs(p.host["vel_y"][3] - (vy0 + 0.5 * (ay0 + ay1) * dt)) <= 1e-6
+        np.testing.assert_array_equal(p.host["acc_old_y"][3], np.float32(ay0))
+        integ.release_state(p.device)
+    calc.close()
