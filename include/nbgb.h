@@ -325,6 +325,41 @@ nbgb_status nbgb_system_read_f64(nbgb_system* sys, double* x, double* y, double*
 nbgb_status nbgb_system_energy(nbgb_system* sys, double* ke, double* pe, double momentum[3]);
 
 /* ---------------------------------------------------------------------------
+ * Checkpoints (Serializer::save / load, src/utils/serialization.cpp:25-75):
+ * the reference's .nbody v1 file, byte-identical to its writer's, written
+ * from and read into device memory through one pinned file image (one write
+ * or read per file).  nbgb_system_save can add an FP64 sidecar <path>.f64
+ * (32-byte header: magic 0x4E424638, version 2, u64 count, 16 zero bytes;
+ * then float64 x, y, z, vx, vy, vz); nbgb_system_load restores the FP64
+ * state from it when every value rounds to the v1 file's float32 value
+ * (*restored_f64 = 1), so a restarted run continues bitwise where the saved
+ * one stood.  Load errors carry the reference's messages.
+ * ------------------------------------------------------------------------- */
+typedef struct nbgb_checkpoint_header {
+  uint64_t particle_count;   /* set by the loaders; ignored on save (the data's count) */
+  float simulation_time;
+  float dt;
+  float G;
+  float softening;
+  uint32_t force_method;     /* nbgb_method */
+} nbgb_checkpoint_header;
+
+/* d_particles: device arrays pos, vel, mass. */
+nbgb_status nbgb_checkpoint_save_device(const char* path, const nbgb_particle_data* d_particles,
+                                        const nbgb_checkpoint_header* hdr, void* stream);
+/* d_particles->count must equal the file's count; d_particles == NULL reads
+ * the header only. */
+nbgb_status nbgb_checkpoint_load_device(const char* path, nbgb_particle_data* d_particles,
+                                        nbgb_checkpoint_header* hdr, void* stream);
+/* Saves the system's state (velocities synchronised to its positions). */
+nbgb_status nbgb_system_save(nbgb_system* sys, const char* path,
+                             const nbgb_checkpoint_header* hdr, int32_t with_f64);
+/* A new system on calc from a checkpoint (a(0) computed as in
+ * nbgb_system_create). */
+nbgb_status nbgb_system_load(nbgb_calculator* calc, const char* path, nbgb_system** out,
+                             nbgb_checkpoint_header* hdr, int32_t* restored_f64);
+
+/* ---------------------------------------------------------------------------
  * Ensemble serving (no reference counterpart; the reference runs one
  * ParticleSystem at a time).  Many independent simulations share the GPU:
  * requests are admitted while the HBM budget and the resident cap allow,

@@ -177,21 +177,7 @@ using namespace nbgb;
 // ---------------------------------------------------------------------------
 constexpr int64_t kPotentialF64MaxN = (int64_t)1 << 18;
 
-struct nbgb_system {
-  nbgb_calculator* calc = nullptr;
-  int64_t n = 0;
-  DevBuf<double> x, y, z, vx, vy, vz;
-  DevBuf<float> ax, ay, az;
-  DevBuf<double> ax64, ay64, az64;  // NBGB_FLAG_FP64: accelerations in FP64
-  DevBuf<float4> pm;
-  DevBuf<double> red;
-  HostPinned<double> h_red;
-  bool fp64 = false;
-  bool pending_half = false;  // v lags x by half a kick of size last_dt/2
-  double last_dt = 0.0;
-};
-
-static void system_sync_velocity(nbgb_system* s) {
+void nbgb::system_sync_velocity(nbgb_system* s) {
   if (!s->pending_half) return;
   if (s->fp64)
     launch_kick(s->n, s->vx.ptr, s->vy.ptr, s->vz.ptr, s->ax64.ptr, s->ay64.ptr, s->az64.ptr,

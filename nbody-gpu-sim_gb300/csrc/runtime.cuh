@@ -98,7 +98,26 @@ struct nbgb_calculator {
   std::unique_ptr<nbgb::HashState, nbgb::HashDeleter> hash;
 };
 
+// A device-resident system (nbgb_system_*): FP64 x, v; FP32 (or FP64) a;
+// packed FP32 (x, y, z, m) for the force kernels.
+struct nbgb_system {
+  nbgb_calculator* calc = nullptr;
+  int64_t n = 0;
+  nbgb::DevBuf<double> x, y, z, vx, vy, vz;
+  nbgb::DevBuf<float> ax, ay, az;
+  nbgb::DevBuf<double> ax64, ay64, az64;  // NBGB_FLAG_FP64: accelerations in FP64
+  nbgb::DevBuf<float4> pm;
+  nbgb::DevBuf<double> red;
+  nbgb::HostPinned<double> h_red;
+  bool fp64 = false;
+  bool pending_half = false;  // v lags x by half a kick of size last_dt/2
+  double last_dt = 0.0;
+};
+
 namespace nbgb {
+
+// Applies a system's pending half kick (v then matches x in time).
+void system_sync_velocity(nbgb_system* s);
 
 // Forces on n bodies given as packed float4 `pm` (padded by the callee's own
 // requirements where needed); writes ax/ay/az (length n).  Enqueued on

@@ -57,6 +57,12 @@ class EnsembleResult(C.Structure):
                 ("method", C.c_int32), ("gpu_ms", C.c_double)]
 
 
+class CheckpointHeader(C.Structure):
+    _fields_ = [("particle_count", C.c_uint64), ("simulation_time", C.c_float),
+                ("dt", C.c_float), ("G", C.c_float), ("softening", C.c_float),
+                ("force_method", C.c_uint32)]
+
+
 class EnsembleStats(C.Structure):
     _fields_ = [("ticks", C.c_int64), ("particle_steps", C.c_int64),
                 ("direct_interactions", C.c_double), ("bh_interactions", C.c_double),
@@ -124,6 +130,11 @@ _SIGS = {
     "nbgb_system_read": (C.c_int, [_vp, _pd]),
     "nbgb_system_read_f64": (C.c_int, [_vp] + [_vp] * 6),
     "nbgb_system_energy": (C.c_int, [_vp, _f64p, _f64p, _f64p]),
+    "nbgb_checkpoint_save_device": (C.c_int, [C.c_char_p, _pd, C.POINTER(CheckpointHeader), _vp]),
+    "nbgb_checkpoint_load_device": (C.c_int, [C.c_char_p, _pd, C.POINTER(CheckpointHeader), _vp]),
+    "nbgb_system_save": (C.c_int, [_vp, C.c_char_p, C.POINTER(CheckpointHeader), C.c_int32]),
+    "nbgb_system_load": (C.c_int, [_vp, C.c_char_p, C.POINTER(_vp), C.POINTER(CheckpointHeader),
+                                   _i32p]),
     "nbgb_measure_fp32_peak": (C.c_int, [_f64p, _f64p, _f64p]),
     "nbgb_direct_f64": (C.c_int, [_vp, C.c_int64, _vp, C.c_int64, C.c_double, C.c_double,
                                   _vp, _vp, _vp, _vp]),

@@ -7,6 +7,11 @@ u64 particle_count, f32 simulation_time, dt, G, softening, u32 force_method,
 pos_x, pos_y, pos_z, vel_x, vel_y, vel_z, mass.  Accelerations are not
 stored.  FP64 state is rounded to float32 on save.
 
+The device functions below move the arrays between device memory and the
+file through one pinned file image (nbgb_checkpoint_*), and save / load a
+device-resident system with an FP64 sidecar <path>.f64 that restores its
+exact state (nbgb_system_save / nbgb_system_load).
+
 Load validates like Serializer::load (serialization.cpp:39-75,111-129):
 truncated header, wrong magic, unsupported version, count above 1e8,
 force method above SPATIAL_HASH and truncated arrays are rejected with the
@@ -15,6 +20,7 @@ reference's messages.
 from __future__ import annotations
 
 import io
+import os
 import struct
 
 import numpy as np
@@ -88,3 +94,70 @@ def to_bytes(state: dict, **kw) -> bytes:
     b = io.BytesIO()
     save(b, state, **kw)
     return b.getvalue()
+
+
+# --- device fast path (nbgb_checkpoint_*, nbgb_system_save / load) -----------
+def _hdr(simulation_time=0.0, dt=1e-3, G=1.0, softening=0.1, force_method=0):
+    from ._lib import CheckpointHeader
+    h = CheckpointHeader()
+    h.simulation_time, h.dt, h.G, h.softening = simulation_time, dt, G, softening
+    h.force_method = int(force_method)
+    return h
+
+
+def _header_dict(h) -> dict:
+    return dict(particle_count=h.particle_count, simulation_time=h.simulation_time, dt=h.dt,
+                G=h.G, softening=h.softening, force_method=h.force_method)
+
+
+def save_device(path, d, **header) -> None:
+    """The v1 file of device ParticleData `d` (pos, vel, mass), written from one
+    pinned file image (the same bytes as save() of the same float32 arrays)."""
+    import ctypes as C
+
+    from . import _lib
+    from .api import check
+    h = _hdr(**header)
+    check(_lib.lib().nbgb_checkpoint_save_device(os.fsencode(path), d.ptr(), C.byref(h), None))
+
+
+def load_device(path, d) -> dict:
+    """Reads a v1 file into device ParticleData `d` (count must match); returns
+    the header.  With d None, reads the header only."""
+    import ctypes as C
+
+    from . import _lib
+    from ._lib import CheckpointHeader
+    from .api import check
+    h = CheckpointHeader()
+    check(_lib.lib().nbgb_checkpoint_load_device(os.fsencode(path), d.ptr() if d else None,
+                                                 C.byref(h), None))
+    return _header_dict(h)
+
+
+def save_system(path, system, with_f64: bool = True, **header) -> None:
+    """A device-resident system's state as v1 (+ the FP64 sidecar <path>.f64)."""
+    import ctypes as C
+
+    from . import _lib
+    from .api import check
+    h = _hdr(**header)
+    check(_lib.lib().nbgb_system_save(system.handle, os.fsencode(path), C.byref(h),
+                                      1 if with_f64 else 0))
+
+
+def load_system(path, calc):
+    """(System, header dict, FP64 state restored?) from a checkpoint."""
+    import ctypes as C
+
+    from . import _lib
+    from ._lib import CheckpointHeader
+    from .api import System, check
+    h = CheckpointHeader()
+    hd = C.c_void_p()
+    restored = C.c_int32(0)
+    check(_lib.lib().nbgb_system_load(calc.handle, os.fsencode(path), C.byref(hd), C.byref(h),
+                                      C.byref(restored)))
+    sysm = System.__new__(System)
+    sysm.calc, sysm.n, sysm.handle = calc, int(h.particle_count), hd
+    return sysm, _header_dict(h), bool(restored.value)
