@@ -136,6 +136,47 @@ def case_arm(args, local):
     return {"case": args.case, "n": n, "ms_per_eval": e0.elapsed_time(e1) / args.steps}
 
 
+def per_config_timings(nbgb) -> dict:
+    """The single-system workloads of the other configurations, timed in the
+    same run (CUDA events over 10 force evaluations after 2 warm-ups, inputs
+    resident): Barnes-Hut on two Plummer spheres N = 1,048,576 (theta 0.5,
+    eps 0.01) with the reference-style walk and with the group walk, one body
+    per leaf and 8-body buckets (the workload's leaf <= 8); the spatial hash
+    on the uniform cube N = 4,194,304 (cell = cutoff = 2)."""
+    import torch
+
+    def timed(calc, s, reps=10):
+        calc.setSofteningParameter(EPS)
+        st = torch.cuda.current_stream()
+        calc.set_stream(st.cuda_stream)
+        n = len(s["x"])
+        with nbgb.ScopedParticleData(n, {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"],
+                                         "mass": s["m"]}) as p:
+            for _ in range(2):
+                calc.computeForces(p.device)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                calc.computeForces(p.device)
+            e1.record(st)
+            torch.cuda.synchronize()
+        calc.close()
+        return e0.elapsed_time(e1) / reps
+
+    out = {}
+    s = nbgb.ics.two_plummer(1 << 20, seed=2)
+    bh = {}
+    for name, leaf, group in (("reference_walk_leaf1", 1, False), ("reference_walk_leaf8", 8, False),
+                              ("group_walk_leaf1", 1, True), ("group_walk_leaf8", 8, True)):
+        bh[name] = timed(nbgb.BarnesHutCalculator(0.5, leaf_capacity=leaf, group_walk=group), s)
+    out["barnes_hut_two_plummer_1048576_ms_per_eval"] = bh
+    del s
+    s = nbgb.ics.uniform_cube(4_194_304, seed=3, side=160.0)
+    out["spatial_hash_uniform_4194304_ms_per_eval"] = timed(nbgb.SpatialHashCalculator(2.0, 2.0), s)
+    return out
+
+
 def integrate_arm(args, local):
     """Achieved HBM bandwidth of the reference-semantics integrator kernels
     (updatePositions, updateVelocities, storeOldAccelerations of
@@ -365,6 +406,7 @@ def gpu_arm(args, rank, world, local):
         # --- CPU baseline (reference CPU path, restated) -------------------------
         cpu = cpu_baseline(nbgb, stream, args.cpu_seconds)
         cpu["direct_n1024_100_steps"] = c1_cpu_baseline(nbgb)
+        per_config = per_config_timings(nbgb)
         force_err = measured_force_error(nbgb)
 
         ffma_peak = ffma.value
@@ -448,6 +490,7 @@ def gpu_arm(args, rank, world, local):
                            "spec_note": "SMs x 128 FP32 lanes x 2 flops x the maximum SM "
                                         "clock (nvidia-smi)"},
             "cpu_baseline": cpu,
+            "per_config": per_config,
             "clocks": clocks,
             "gpu_launches": launches,
         }

@@ -4,9 +4,10 @@
   ``-ffp-contract=off`` (see that file's header) and OpenMP.
 * ``oracle/_ref/libnbody_ref.so``: the reference's own host-side code,
   compiled in place from the reference sources plus ``ref_harness.cpp``.  Only
-  built where the reference tree exists; outputs go to ``oracle/_ref/`` only.
+  built where NBGB_REFERENCE_ROOT names the reference tree; outputs go to
+  ``oracle/_ref/`` only.
 
-Usage: ``python oracle/build.py [--ref]``.
+Usage: ``NBGB_REFERENCE_ROOT=<reference tree> python oracle/build.py [--ref]``.
 """
 from __future__ import annotations
 
@@ -16,7 +17,11 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("NBGB_REFERENCE_ROOT", "/root/reference")
+# The reference tree is named by NBGB_REFERENCE_ROOT; a build of
+# oracle/_ref records the tree it used (oracle/_ref/source_root), so later
+# processes find it without the variable.  Without either, only an already
+# built oracle/_ref library is used.
+REF_ROOT = os.environ.get("NBGB_REFERENCE_ROOT", "")
 LIB = os.path.join(HERE, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_LIB = os.path.join(REF_DIR, "libnbody_ref.so")
@@ -54,20 +59,32 @@ def build_oracle(force: bool = False) -> str:
     return LIB
 
 
+def _ref_root() -> str:
+    root = os.environ.get("NBGB_REFERENCE_ROOT", REF_ROOT)
+    rec = os.path.join(REF_DIR, "source_root")
+    if not root and os.path.isfile(rec):
+        with open(rec) as f:
+            root = f.read().strip()
+    return root
+
+
 def reference_available() -> bool:
-    return os.path.isfile(os.path.join(REF_ROOT, "src/cuda/force_barnes_hut.cu"))
+    root = _ref_root()
+    return bool(root) and os.path.isfile(os.path.join(root, "src/cuda/force_barnes_hut.cu"))
 
 
 def build_ref(force: bool = False) -> str | None:
-    """Compile the reference host code + harness into oracle/_ref (CPU use only)."""
+    """Compile the reference host code + harness into oracle/_ref (CPU use only).
+    Without the reference sources, an earlier build of the library is used."""
     if not reference_available():
-        return None
+        return REF_LIB if os.path.isfile(REF_LIB) else None
+    root = _ref_root()
     harness = os.path.join(HERE, "ref_harness.cpp")
-    srcs = [os.path.join(REF_ROOT, s) for s in _REF_CU + _REF_CPP] + [harness]
+    srcs = [os.path.join(root, s) for s in _REF_CU + _REF_CPP] + [harness]
     if not (force or _stale(REF_LIB, srcs)):
         return REF_LIB
     os.makedirs(REF_DIR, exist_ok=True)
-    inc = ["-I", os.path.join(REF_ROOT, "include")]
+    inc = ["-I", os.path.join(root, "include")]
     # The reference is built with separable compilation (its CMakeLists sets
     # CUDA_SEPARABLE_COMPILATION); the kernels are compiled but never run here.
     nv = ["nvcc", "-std=c++17", "-O3", "-rdc=true", "-Xcompiler", "-fPIC",
@@ -76,11 +93,11 @@ def build_ref(force: bool = False) -> str | None:
     jobs, objs = [], []
     for s in _REF_CU:
         o = os.path.join(REF_DIR, os.path.basename(s) + ".o")
-        jobs.append(nv + ["-c", os.path.join(REF_ROOT, s), "-o", o])
+        jobs.append(nv + ["-c", os.path.join(root, s), "-o", o])
         objs.append(o)
     for s in _REF_CPP:
         o = os.path.join(REF_DIR, os.path.basename(s) + ".o")
-        jobs.append(gx + ["-c", os.path.join(REF_ROOT, s), "-o", o])
+        jobs.append(gx + ["-c", os.path.join(root, s), "-o", o])
         objs.append(o)
     ho = os.path.join(REF_DIR, "ref_harness.o")
     jobs.append(gx + ["-c", harness, "-o", ho])
@@ -89,6 +106,8 @@ def build_ref(force: bool = False) -> str | None:
         list(ex.map(_run, jobs))
     _run(["nvcc", "-shared", "-rdc=true", "-gencode", "arch=compute_103a,code=sm_103a",
           "-cudart", "shared", "-Xlinker", "-Bsymbolic", *objs, "-o", REF_LIB])
+    with open(os.path.join(REF_DIR, "source_root"), "w") as f:
+        f.write(root + "\n")
     return REF_LIB
 
 
@@ -100,10 +119,11 @@ def link_reference_apps(lib_dir: str) -> dict[str, str] | None:
     Returns {app: path} or None where the reference sources are absent."""
     if not reference_available():
         return None
+    root = _ref_root()
     repo = os.path.dirname(HERE)
     out = os.path.join(REF_DIR, "link")
     os.makedirs(out, exist_ok=True)
-    inc = ["-I", os.path.join(REF_ROOT, "include"), "-I", os.path.join(repo, "include"),
+    inc = ["-I", os.path.join(root, "include"), "-I", os.path.join(repo, "include"),
            "-I", "/usr/local/cuda/include"]
     defs = ["-DNDEBUG", "-DNBODY_WITH_CUDA=1", "-DNBODY_WITH_RENDERING=0", "-DNBODY_WITH_UI=0",
             "-DNBODY_ENABLE_PROFILING=1"]
@@ -114,13 +134,13 @@ def link_reference_apps(lib_dir: str) -> dict[str, str] | None:
     for s in srcs:
         o = os.path.join(out, os.path.basename(s) + ".o")
         jobs.append(["g++", "-std=c++17", "-O2", "-fPIC"] + defs + inc +
-                    ["-c", os.path.join(REF_ROOT, s), "-o", o])
+                    ["-c", os.path.join(root, s), "-o", o])
         objs.append(o)
     # particle_init.cu holds host code only (allocation, copies, initialisers)
     o = os.path.join(out, "particle_init.cu.o")
     jobs.append(["nvcc", "-std=c++17", "-O2", "-Xcompiler", "-fPIC",
                  "-gencode", "arch=compute_103a,code=sm_103a"] + defs + inc +
-                ["-c", os.path.join(REF_ROOT, "src/cuda/particle_init.cu"), "-o", o])
+                ["-c", os.path.join(root, "src/cuda/particle_init.cu"), "-o", o])
     objs.append(o)
     ad = os.path.join(out, "nbody_adapter.o")
     jobs.append(["g++", "-std=c++17", "-O2", "-fPIC"] + defs + inc +
@@ -131,7 +151,7 @@ def link_reference_apps(lib_dir: str) -> dict[str, str] | None:
              "example_basic": "examples/example_basic.cpp"}
     for app, s in mains.items():
         jobs.append(["g++", "-std=c++17", "-O2", "-fPIC"] + defs + inc +
-                    ["-c", os.path.join(REF_ROOT, s), "-o", os.path.join(out, app + ".o")])
+                    ["-c", os.path.join(root, s), "-o", os.path.join(out, app + ".o")])
     with ThreadPoolExecutor(max_workers=8) as ex:
         list(ex.map(_run, jobs))
     apps = {}
