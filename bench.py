@@ -73,6 +73,8 @@ def parse():
     ap.add_argument("--case-n", type=int, default=None,
                     help="bodies of a --case run (262144; 33554432 for integrate)")
     ap.add_argument("--precision-steps", type=int, default=2000)
+    ap.add_argument("--precision-fp64-steps", type=int, default=16,
+                    help="steps of the three-variant run at the full N of --case precision")
     return ap.parse_args()
 
 
@@ -81,7 +83,9 @@ def precision_arm(args, local) -> dict:
     force error of FP32 plain and FP32 compensated against the FP64 direct
     sum at N=262144 (4096 seeded targets); energy drift over 2000 steps of
     both FP32 variants at N=262144 and of all three variants (with full
-    FP64) at N=16384, where FP64 arithmetic fits the time budget."""
+    FP64) at N=16384, where FP64 arithmetic fits the time budget; and all
+    three variants at N=262144 over a reduced step count
+    (--precision-fp64-steps, 16 by default: one FP64 step takes ~5 s there)."""
     import torch
 
     import nbgb.precision as prec
@@ -93,6 +97,9 @@ def precision_arm(args, local) -> dict:
            "energy_full_n": prec.energy_drift(n, eps, dt, steps,
                                               variants=("fp32", "fp32c_fp64")),
            "energy_small_n": prec.energy_drift(16384, eps, dt, steps)}
+    if args.precision_fp64_steps > 0:
+        out["energy_full_n_all_variants"] = prec.energy_drift(n, eps, dt,
+                                                              args.precision_fp64_steps)
     return out
 
 

@@ -105,8 +105,9 @@ typedef struct nbgb_params {
  * accelerations kept in FP64 (the full-FP64 reference variant; FP64
  * arithmetic runs at a small fraction of the FP32 rate on GB300). */
 #define NBGB_FLAG_FP64 0x8u
-/* Barnes-Hut group walk: the bodies of each small subtree (at most 32,
- * consecutive small sibling subtrees merged) share one interaction list; a
+/* Barnes-Hut group walk: the bodies of each small subtree (at most 32, or 64
+ * in builds of 262,144 bodies or more -- nbgb_bh_group_size; consecutive
+ * small sibling subtrees merged) share one interaction list; a
  * cell is accepted for the group when its cube does not touch the group's
  * bounding box and 4h^2 < theta^2 (d^2 + eps^2), d the distance from the
  * cell's centre of mass to the box.  Every accepted cell passes the
@@ -116,6 +117,12 @@ typedef struct nbgb_params {
  * node of at most that many bodies that is not accepted adds its bodies to
  * the list instead of being opened (buckets). */
 #define NBGB_FLAG_GROUP_WALK 0x10u
+
+/* The largest group of the group walk in a tree build over `count` bodies
+ * (all systems of one batched build together): 32, or 64 from 262,144
+ * bodies on, where each lane of a group's warp sums two bodies.  Host-only;
+ * no reference counterpart. */
+int32_t nbgb_bh_group_size(uint64_t count);
 
 void nbgb_params_default(nbgb_params* p);
 
@@ -365,9 +372,10 @@ nbgb_status nbgb_system_load(nbgb_calculator* calc, const char* path, nbgb_syste
  * requests are admitted while the HBM budget and the resident cap allow,
  * every resident system advances one Velocity-Verlet step per tick (FP64
  * x/v state, FP32 forces: direct sum for N <= direct_max_n through one
- * persistent work-queue kernel spanning all direct systems, Barnes-Hut per
- * system as a CUDA graph on a stream pool), and finished systems retire and
- * free their memory.  The result of a system does not depend on what else
+ * persistent work-queue kernel spanning all direct systems; Barnes-Hut for
+ * all resident systems as one segmented tree build, captured as a CUDA graph
+ * once the resident set is stable, and one batched walk on a side stream),
+ * and finished systems retire and free their memory.  The result of a system does not depend on what else
  * is resident (per-system work decomposition), except through the direct
  * kernel configuration the autotuner picks (rounding-level differences).
  * ------------------------------------------------------------------------- */

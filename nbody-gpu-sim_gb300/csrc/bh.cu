@@ -511,14 +511,15 @@ struct GroupSink {
   const int32_t* seg_of;
   int4* groups;          // first body, count, segment
   GroupCounters* gc;
+  int gmax;              // largest group (32 or 64 bodies)
 };
 
 // Parent links and child counts (children of P: P+1, skip(P+1), ... < skip(P)).
 // With GROUPS it also emits the group walk's groups: roots with at most
-// kGroupSize bodies; below larger nodes, runs of consecutive children with
-// at most kGroupSize bodies in total (merged only when the parent holds at
-// most kGroupMergeMax bodies: sibling cells of a large sparse node can lie
-// far apart); depth-32 leaves larger than a group are split.  Every body
+// gmax bodies; below larger nodes, runs of consecutive children with at
+// most gmax bodies in total (merged only when the parent holds at most
+// kGroupMergeMax bodies: sibling cells of a large sparse node can lie far
+// apart); depth-32 leaves larger than a group are split.  Every body
 // belongs to exactly one group, and a group is one contiguous range of
 // path-sorted bodies.
 template <bool GROUPS>
@@ -527,6 +528,7 @@ __global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __re
                             int32_t* __restrict__ nchild, GroupSink gs) {
   const uint32_t total = nstart[n];
   if ((int64_t)total > cap) return;
+  const int gmax = gs.gmax;
   auto emit = [&](int f, int c) {
     const uint32_t g = atomicAdd(&gs.gc->ngroups, 1u);
     gs.groups[g] = make_int4(f, c, gs.seg_of[gs.body[f]], 0);
@@ -536,22 +538,22 @@ __global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __re
     const int4 ip = nodes[p].info;  // skip, depth << 8 | leaf, first, count
     if (ip.y & 1) {
       nchild[p] = 0;
-      if (GROUPS && ip.w > kGroupSize)
-        for (int f = 0; f < ip.w; f += kGroupSize) emit(ip.z + f, min(kGroupSize, ip.w - f));
+      if (GROUPS && ip.w > gmax)
+        for (int f = 0; f < ip.w; f += gmax) emit(ip.z + f, min(gmax, ip.w - f));
       continue;
     }
-    if (GROUPS && (ip.y >> 8) == 0 && ip.w <= kGroupSize) emit(ip.z, ip.w);  // a small root
-    const bool grp = GROUPS && ip.w > kGroupSize, merge = ip.w <= kGroupMergeMax;
+    if (GROUPS && (ip.y >> 8) == 0 && ip.w <= gmax) emit(ip.z, ip.w);  // a small root
+    const bool grp = GROUPS && ip.w > gmax, merge = ip.w <= kGroupMergeMax;
     int c = (int)p + 1, nc = 0, gf = 0, gn = 0;
     while (c < ip.x) {
       parent[c] = (int)p;
       ++nc;
       const int4 ci = nodes[c].info;
       if (grp) {
-        if (ci.w > kGroupSize) {
+        if (ci.w > gmax) {
           if (gn) emit(gf, gn);
           gn = 0;
-        } else if (gn && merge && gn + ci.w <= kGroupSize) {
+        } else if (gn && merge && gn + ci.w <= gmax) {
           gn += ci.w;
         } else {
           if (gn) emit(gf, gn);
@@ -947,8 +949,10 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   internal_nodes_kernel<<<grid1d(h.cap), 256, 0, st>>>(ea);
   NBGB_LAUNCH_CHECK();
   if (groups) {
+    h.group_max = bh_group_max(n);
     GroupSink gs{h.body, h.seg_of.ptr, grow(h.groups, R),
-                 reinterpret_cast<GroupCounters*>(grow(h.group_ctr, sizeof(GroupCounters)))};
+                 reinterpret_cast<GroupCounters*>(grow(h.group_ctr, sizeof(GroupCounters))),
+                 h.group_max};
     NBGB_CUDA(cudaMemsetAsync(gs.gc, 0, sizeof(GroupCounters), st));
     link_kernel<true><<<grid1d(h.cap), 256, 0, st>>>(nodes, nst, n, h.cap, par, nch, gs);
   } else {
@@ -957,7 +961,8 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   NBGB_LAUNCH_CHECK();
   h.groups_ready = groups;
   // one thread per node slot: a leaf thread carries centres of mass up the
-  // tree, so slots are not chained per thread
+  // tree, so slots are not chained per thread (one resident wave of threads
+  // striding over the slots was 0.3 ms per serving tick slower)
   com_kernel<<<(unsigned)ceil_div(h.cap, 256), 256, 0, st>>>(nodes, spm, nst, n, h.cap, par, nch,
                                                             vis);
   NBGB_LAUNCH_CHECK();
@@ -1192,6 +1197,10 @@ nbgb_status nbgb_copy_interaction_counts(nbgb_calculator* c, int32_t* counts, si
   return cudaMemcpy(counts, c->counts.ptr, n * 4, cudaMemcpyDeviceToHost) == cudaSuccess
              ? NBGB_OK
              : NBGB_ERR_CUDA;
+}
+
+int32_t nbgb_bh_group_size(uint64_t count) {
+  return nbgb::bh_group_max(count > (uint64_t)INT64_MAX ? INT64_MAX : (int64_t)count);
 }
 
 }  // extern "C"

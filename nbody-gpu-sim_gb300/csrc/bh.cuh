@@ -21,7 +21,7 @@ struct BHWalkParams {
   float softening;
   float theta;
   int leaf_capacity;  // > 1: subtrees of at most this many bodies are summed body by body
-  int group_walk;     // 1: one interaction list per group of <= 32 nearby bodies, cells
+  int group_walk;     // 1: one interaction list per group of <= 64 nearby bodies, cells
                       // accepted by the group's bounding box (opened buckets of at most
                       // leaf_capacity bodies list their bodies)
 };

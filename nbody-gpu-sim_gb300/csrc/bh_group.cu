@@ -12,7 +12,7 @@ namespace nbgb {
 
 // ---------------------------------------------------------- group walk --
 // Barnes-Hut with a per-group opening test: the bodies of one small subtree
-// (or of consecutive small sibling subtrees, at most 32 bodies) share one
+// (or of consecutive small sibling subtrees, at most 64 bodies) share one
 // interaction list, built by one warp that tests 32 nodes at a time.  A cell
 // is accepted for the whole group when its cube does not touch the group's
 // bounding box and size2 < theta2 (d_min^2 + eps^2), d_min being the distance
@@ -23,7 +23,8 @@ namespace nbgb {
 // node of at most that many bodies that is not accepted contributes its
 // bodies instead of being opened (buckets).  The list is evaluated by
 // all lanes at once, one target per lane (2 or 4 lanes per target in groups
-// of at most 16 or 8 bodies), in packed FP32x2 arithmetic.
+// of at most 16 or 8 bodies, two targets per lane in groups of more than 32),
+// in packed FP32x2 arithmetic.
 struct GroupWalkArgs {
   const Node* nodes;
   const float4* spm;
@@ -59,6 +60,32 @@ __device__ __forceinline__ float float_of(uint32_t o) {
   return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
 }
 
+// One pair of list entries (packed x, y, z, m) added to one target.
+template <bool ZERO_EPS>
+__device__ __forceinline__ void pair_add(f2 xj, f2 yj, f2 zj, f2 m, f2 px, f2 py, f2 pz, f2 e2,
+                                         f2& ax2, f2& ay2, f2& az2) {
+  const f2 dx = f2_sub(xj, px);
+  const f2 dy = f2_sub(yj, py);
+  const f2 dz = f2_sub(zj, pz);
+  const f2 d2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, e2)));
+  float d2l, d2h;
+  f2_split(d2, d2l, d2h);
+  float rl = rsqrt_approx(d2l), rh = rsqrt_approx(d2h);
+  if (ZERO_EPS) {  // coincident bodies (and the target itself) add nothing
+    rl = d2l > 0.0f ? rl : 0.0f;
+    rh = d2h > 0.0f ? rh : 0.0f;
+  }
+  const f2 rr = f2_make(rl, rh);
+  const f2 f = f2_mul(f2_mul(m, rr), f2_mul(rr, rr));
+  ax2 = f2_fma(f, dx, ax2);
+  ay2 = f2_fma(f, dy, ay2);
+  az2 = f2_fma(f, dz, az2);
+}
+
+__device__ __forceinline__ f2 ring_pair(const float* e, int j) {
+  return f2{*reinterpret_cast<const unsigned long long*>(e + j)};
+}
+
 // Adds list entries [base, base + cnt) of the ring (cnt a multiple of 4)
 // to the lane's target, two entries per packed operation.  With rep > 1
 // lanes per body (small groups), replica r takes every rep-th pair.
@@ -72,35 +99,40 @@ __device__ __forceinline__ void group_eval(const float* ex, const float* ey, con
   // entries are read as pairs straight into packed registers
   const int j0 = FULL ? 0 : 2 * r, jn = FULL ? 32 : cnt, js = FULL ? 2 : 2 * rep;
 #pragma unroll(FULL ? 16 : 1)
-  for (int j = j0; j < jn; j += js) {
-    const f2 xj{*reinterpret_cast<const unsigned long long*>(ex + base + j)};
-    const f2 yj{*reinterpret_cast<const unsigned long long*>(ey + base + j)};
-    const f2 zj{*reinterpret_cast<const unsigned long long*>(ez + base + j)};
-    const f2 m{*reinterpret_cast<const unsigned long long*>(em + base + j)};
-    const f2 dx = f2_sub(xj, px);
-    const f2 dy = f2_sub(yj, py);
-    const f2 dz = f2_sub(zj, pz);
-    const f2 d2 = f2_fma(dx, dx, f2_fma(dy, dy, f2_fma(dz, dz, e2)));
-    float d2l, d2h;
-    f2_split(d2, d2l, d2h);
-    float rl = rsqrt_approx(d2l), rh = rsqrt_approx(d2h);
-    if (ZERO_EPS) {  // coincident bodies (and the target itself) add nothing
-      rl = d2l > 0.0f ? rl : 0.0f;
-      rh = d2h > 0.0f ? rh : 0.0f;
-    }
-    const f2 rr = f2_make(rl, rh);
-    const f2 f = f2_mul(f2_mul(m, rr), f2_mul(rr, rr));
-    ax2 = f2_fma(f, dx, ax2);
-    ay2 = f2_fma(f, dy, ay2);
-    az2 = f2_fma(f, dz, az2);
+  for (int j = j0; j < jn; j += js)
+    pair_add<ZERO_EPS>(ring_pair(ex, base + j), ring_pair(ey, base + j), ring_pair(ez, base + j),
+                       ring_pair(em, base + j), px, py, pz, e2, ax2, ay2, az2);
+}
+
+// Groups of 33..64 bodies: two targets per lane (bodies lane and lane + 32),
+// each pair of entries read from the ring once and added to both, which
+// halves the shared-memory reads per interaction.
+template <bool ZERO_EPS, bool FULL>
+__device__ __forceinline__ void group_eval2(const float* ex, const float* ey, const float* ez,
+                                            const float* em, int base, int cnt, float4 pi,
+                                            float4 pj, float eps2, f2& ax2, f2& ay2, f2& az2,
+                                            f2& bx2, f2& by2, f2& bz2) {
+  const f2 px = f2_make(pi.x, pi.x), py = f2_make(pi.y, pi.y), pz = f2_make(pi.z, pi.z);
+  const f2 qx = f2_make(pj.x, pj.x), qy = f2_make(pj.y, pj.y), qz = f2_make(pj.z, pj.z);
+  const f2 e2 = f2_make(eps2, eps2);
+  const int jn = FULL ? 32 : cnt;
+#pragma unroll(FULL ? 8 : 1)
+  for (int j = 0; j < jn; j += 2) {
+    const f2 xj = ring_pair(ex, base + j), yj = ring_pair(ey, base + j),
+             zj = ring_pair(ez, base + j), m = ring_pair(em, base + j);
+    pair_add<ZERO_EPS>(xj, yj, zj, m, px, py, pz, e2, ax2, ay2, az2);
+    pair_add<ZERO_EPS>(xj, yj, zj, m, qx, qy, qz, e2, bx2, by2, bz2);
   }
 }
 
 // CNT: 0 no counting; 1 the total only (list lengths minus one per body of
 // nonzero mass, whose own leaf is in its list); 2 exact per-body counts (the
 // own leaf tracked as it is listed) and their total.
-template <int CNT, bool ZERO_EPS>
-__global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kernel(GroupWalkArgs a) {
+// TWO: groups of up to 64 bodies (two targets per lane above 32; 80
+// registers, 3 blocks per SM); otherwise groups of up to 32 (64 registers,
+// 4 blocks per SM).
+template <int CNT, bool ZERO_EPS, bool TWO>
+__global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kernel(GroupWalkArgs a) {
   constexpr bool COUNT = CNT == 2;
   __shared__ int s_stack[kGWarps][kGStack];
   __shared__ __align__(16) float s_ring[kGWarps][4][kGRing];
@@ -123,19 +155,22 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
     if (t >= ngroups) break;
     const int4 g = a.groups[t];  // first, count, segment
     // a group of at most 8 (16) bodies gives each body 4 (2) lanes, each
-    // summing a share of the list: lane = replica * gw + body
+    // summing a share of the list: lane = replica * gw + body; a group of
+    // more than 32 bodies gives each lane two (lane and lane + 32)
+    const bool two = TWO && g.y > 32;
     const int gw = g.y <= 8 ? 8 : (g.y <= 16 ? 16 : 32);
     const int rep = 32 / gw, tl = lane & (gw - 1), rr = lane / gw;
-    const bool valid = tl < g.y;
-    const int k = g.x + (valid ? tl : 0);
+    const bool valid = tl < g.y, valid2 = two && lane + 32 < g.y;
+    const int k = g.x + (valid ? tl : 0), k2 = g.x + (valid2 ? lane + 32 : 0);
     const float4 pi = a.spm[k];
+    const float4 pj = two ? a.spm[k2] : pi;  // invalid second bodies repeat body 0
     {
-      const float lox = float_of(__reduce_min_sync(full, ord_of(pi.x)));
-      const float loy = float_of(__reduce_min_sync(full, ord_of(pi.y)));
-      const float loz = float_of(__reduce_min_sync(full, ord_of(pi.z)));
-      const float hix = float_of(__reduce_max_sync(full, ord_of(pi.x)));
-      const float hiy = float_of(__reduce_max_sync(full, ord_of(pi.y)));
-      const float hiz = float_of(__reduce_max_sync(full, ord_of(pi.z)));
+      const float lox = float_of(__reduce_min_sync(full, min(ord_of(pi.x), ord_of(pj.x))));
+      const float loy = float_of(__reduce_min_sync(full, min(ord_of(pi.y), ord_of(pj.y))));
+      const float loz = float_of(__reduce_min_sync(full, min(ord_of(pi.z), ord_of(pj.z))));
+      const float hix = float_of(__reduce_max_sync(full, max(ord_of(pi.x), ord_of(pj.x))));
+      const float hiy = float_of(__reduce_max_sync(full, max(ord_of(pi.y), ord_of(pj.y))));
+      const float hiz = float_of(__reduce_max_sync(full, max(ord_of(pi.z), ord_of(pj.z))));
       if (lane == 0) {  // centre and half sizes, the halves widened past rounding
         const float cx = __fmul_rn(__fadd_rn(lox, hix), 0.5f);
         const float cy = __fmul_rn(__fadd_rn(loy, hiy), 0.5f);
@@ -147,9 +182,25 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
             __fmul_rn(fmaxf(__fsub_rn(hiz, cz), __fsub_rn(cz, loz)), kBoxWiden), 0.f);
       }
     }
-    f2 ax2 = f2_make(0.f, 0.f), ay2 = ax2, az2 = ax2;
+    f2 ax2 = f2_make(0.f, 0.f), ay2 = ax2, az2 = ax2, bx2 = ax2, by2 = ax2, bz2 = ax2;
     uint32_t wr = 0, rd = 0;  // list entries written / evaluated
-    uint32_t selfmask = 0;    // bodies (by index in the group) whose own leaf is in the list
+    uint64_t selfmask = 0;    // bodies (by index in the group) whose own leaf is in the list
+    // evaluates ring entries [base, base + cnt); full: a whole 32-entry chunk
+    auto eval = [&](int base, int cnt, bool full_chunk) {
+      if (two) {
+        if (full_chunk)
+          group_eval2<ZERO_EPS, true>(ex, ey, ez, em, base, 32, pi, pj, a.eps2, ax2, ay2, az2,
+                                      bx2, by2, bz2);
+        else
+          group_eval2<ZERO_EPS, false>(ex, ey, ez, em, base, cnt, pi, pj, a.eps2, ax2, ay2,
+                                       az2, bx2, by2, bz2);
+      } else if (full_chunk && rep == 1) {
+        group_eval<ZERO_EPS, true>(ex, ey, ez, em, base, 32, 0, 1, pi, a.eps2, ax2, ay2, az2);
+      } else {
+        group_eval<ZERO_EPS, false>(ex, ey, ez, em, base, cnt, rr, rep, pi, a.eps2, ax2, ay2,
+                                    az2);
+      }
+    };
     int sp = 1, gsp = 0;
     bool failed = false;
     if (lane == 0) stk[0] = a.seg_root[g.z];
@@ -237,16 +288,11 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
       wr += __popc(be);
       if (COUNT) {  // lane-local here, combined over the warp at the end
         const uint32_t rel = (uint32_t)(w.z - g.x);
-        if (entry && (wx & kWalkLeaf) && rel < (uint32_t)g.y) selfmask |= 1u << rel;
+        if (entry && (wx & kWalkLeaf) && rel < (uint32_t)g.y) selfmask |= 1ull << rel;
       }
       __syncwarp();
       if (wr - rd >= 32) {
-        if (rep == 1)
-          group_eval<ZERO_EPS, true>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, 0, 1, pi,
-                                     a.eps2, ax2, ay2, az2);
-        else
-          group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi,
-                                      a.eps2, ax2, ay2, az2);
+        eval((int)(rd & (kGRing - 1)), 32, true);
         rd += 32;
         __syncwarp();
       }
@@ -257,7 +303,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
         const int left = small ? cnt : 0;
         if (COUNT && small) {  // the group's bodies inside this run list themselves
           const int lo = max(w.z, g.x), hi = min(w.z + cnt, g.x + g.y);
-          if (lo < hi) selfmask |= ((1u << (hi - lo)) - 1u) << (lo - g.x);
+          if (lo < hi) selfmask |= ((1ull << (hi - lo)) - 1ull) << (lo - g.x);
         }
         for (int j = 0;; ++j) {
           const bool e = j < left;
@@ -274,12 +320,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
           wr += __popc(bj);
           __syncwarp();
           if (wr - rd >= 32) {
-            if (rep == 1)
-              group_eval<ZERO_EPS, true>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, 0, 1, pi,
-                                         a.eps2, ax2, ay2, az2);
-            else
-              group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep,
-                                          pi, a.eps2, ax2, ay2, az2);
+            eval((int)(rd & (kGRing - 1)), 32, true);
             rd += 32;
             __syncwarp();
           }
@@ -293,8 +334,9 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
         bm &= bm - 1;
         const int f = __shfl_sync(full, w.z, src), c = __shfl_sync(full, cnt, src);
         if (COUNT) {
-          const uint32_t o = (uint32_t)(k - f);
-          if (valid && rr == 0 && o < (uint32_t)c) selfmask |= 1u << tl;
+          const uint32_t o = (uint32_t)(k - f), o2 = (uint32_t)(k2 - f);
+          if (valid && rr == 0 && o < (uint32_t)c) selfmask |= 1ull << tl;
+          if (valid2 && o2 < (uint32_t)c) selfmask |= 1ull << (lane + 32);
         }
         for (int b = 0; b < c; b += 32) {
           const bool e = b + lane < c;
@@ -309,8 +351,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
           wr += (uint32_t)min(32, c - b);
           __syncwarp();
           if (wr - rd >= 32) {
-            group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), 32, rr, rep, pi,
-                                        a.eps2, ax2, ay2, az2);
+            eval((int)(rd & (kGRing - 1)), 32, false);
             rd += 32;
             __syncwarp();
           }
@@ -320,7 +361,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
     if (failed) {
       if (lane == 0) raise_error(a.err, kErrWalkStack);
       const float nan = __int_as_float(0x7fc00000);
-      ax2 = ay2 = az2 = f2_make(nan, nan);
+      ax2 = ay2 = az2 = bx2 = by2 = bz2 = f2_make(nan, nan);
     } else {
       // the rest of the list, padded to a multiple of 4 with massless entries
       const int left = (int)(wr - rd), padded = (left + 3) & ~3;
@@ -332,9 +373,7 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
         em[slot] = 0.0f;
       }
       __syncwarp();
-      if (padded)
-        group_eval<ZERO_EPS, false>(ex, ey, ez, em, (int)(rd & (kGRing - 1)), padded, rr, rep, pi,
-                                    a.eps2, ax2, ay2, az2);
+      if (padded) eval((int)(rd & (kGRing - 1)), padded, false);
       __syncwarp();
     }
     for (int o = gw; o < 32; o <<= 1) {  // add up the replicas of each body
@@ -342,8 +381,11 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
       ay2 = f2_add(ay2, f2_shfl_xor(ay2, o));
       az2 = f2_add(az2, f2_shfl_xor(az2, o));
     }
-    if (COUNT) selfmask = __reduce_or_sync(full, selfmask);
+    if (COUNT)
+      selfmask = (uint64_t)__reduce_or_sync(full, (uint32_t)selfmask) |
+                 ((uint64_t)__reduce_or_sync(full, (uint32_t)(selfmask >> 32)) << 32);
     const int cnt_lane = (int)wr - (int)((selfmask >> tl) & 1u);
+    const int cnt_lane2 = (int)wr - (int)((selfmask >> (lane + 32)) & 1u);
     const bool owner = valid && rr == 0;
     if (owner) {
       float sx0, sx1, sy0, sy1, sz0, sz1;
@@ -356,9 +398,22 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
       a.az[i] = a.G * (sz0 + sz1);
       if (COUNT && a.counts) a.counts[i] = cnt_lane;
     }
+    if (valid2) {
+      float sx0, sx1, sy0, sy1, sz0, sz1;
+      f2_split(bx2, sx0, sx1);
+      f2_split(by2, sy0, sy1);
+      f2_split(bz2, sz0, sz1);
+      const int64_t i = a.sv.arena(a.body[k2]);
+      a.ax[i] = a.G * (sx0 + sx1);
+      a.ay[i] = a.G * (sy0 + sy1);
+      a.az[i] = a.G * (sz0 + sz1);
+      if (COUNT && a.counts) a.counts[i] = cnt_lane2;
+    }
     if (CNT > 0 && a.inter_total) {
       const int own = CNT == 2 ? cnt_lane : (int)wr - (pi.w != 0.0f ? 1 : 0);
-      unsigned long long c = owner ? (unsigned long long)own : 0ull;
+      const int own2 = CNT == 2 ? cnt_lane2 : (int)wr - (pj.w != 0.0f ? 1 : 0);
+      unsigned long long c = (owner ? (unsigned long long)own : 0ull) +
+                             (valid2 ? (unsigned long long)own2 : 0ull);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(full, c, o);
       if (lane == 0) atomicAdd(a.inter_total, c);
@@ -366,24 +421,33 @@ __global__ void __launch_bounds__(kGWarps * 32, 32 / kGWarps) bh_group_walk_kern
   }
 }
 
-template <int CNT, bool ZERO_EPS>
+template <int CNT, bool ZERO_EPS, bool TWO>
 static int group_walk_occupancy() {
   static const int occ = [] {
     int b = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bh_group_walk_kernel<CNT, ZERO_EPS>, kGWarps * 32,
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, bh_group_walk_kernel<CNT, ZERO_EPS, TWO>,
+                                                  kGWarps * 32,
                                                   0);
     return std::max(b, 1);
   }();
   return occ;
 }
 
-template <int CNT, bool ZERO_EPS>
-static void launch_group_walk(const GroupWalkArgs& g, int64_t n, cudaStream_t st) {
+template <int CNT, bool ZERO_EPS, bool TWO>
+static void launch_group_walk_t(const GroupWalkArgs& g, int64_t n, cudaStream_t st) {
   // persistent warps: one resident wave, never more warps than bodies
   const int64_t blocks = std::max<int64_t>(
       1, std::min<int64_t>(ceil_div(n, kGWarps),
-                           (int64_t)num_sms() * group_walk_occupancy<CNT, ZERO_EPS>()));
-  bh_group_walk_kernel<CNT, ZERO_EPS><<<(unsigned)blocks, kGWarps * 32, 0, st>>>(g);
+                           (int64_t)num_sms() * group_walk_occupancy<CNT, ZERO_EPS, TWO>()));
+  bh_group_walk_kernel<CNT, ZERO_EPS, TWO><<<(unsigned)blocks, kGWarps * 32, 0, st>>>(g);
+}
+
+template <int CNT, bool ZERO_EPS>
+static void launch_group_walk(const GroupWalkArgs& g, int64_t n, bool two, cudaStream_t st) {
+  if (two)
+    launch_group_walk_t<CNT, ZERO_EPS, true>(g, n, st);
+  else
+    launch_group_walk_t<CNT, ZERO_EPS, false>(g, n, st);
 }
 
 // Shared stack entries the group walk uses before spilling to global memory
@@ -428,21 +492,22 @@ void bh_group_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, floa
   g.leaf_cap = p.leaf_capacity;
   const int cnt = counts ? 2 : (inter_total ? 1 : 0);
   const bool zero_eps = g.eps2 == 0.0f;
+  const bool two = h.group_max > 32;
   if (cnt == 2) {
     if (zero_eps)
-      launch_group_walk<2, true>(g, n, st);
+      launch_group_walk<2, true>(g, n, two, st);
     else
-      launch_group_walk<2, false>(g, n, st);
+      launch_group_walk<2, false>(g, n, two, st);
   } else if (cnt == 1) {
     if (zero_eps)
-      launch_group_walk<1, true>(g, n, st);
+      launch_group_walk<1, true>(g, n, two, st);
     else
-      launch_group_walk<1, false>(g, n, st);
+      launch_group_walk<1, false>(g, n, two, st);
   } else {
     if (zero_eps)
-      launch_group_walk<0, true>(g, n, st);
+      launch_group_walk<0, true>(g, n, two, st);
     else
-      launch_group_walk<0, false>(g, n, st);
+      launch_group_walk<0, false>(g, n, two, st);
   }
   NBGB_LAUNCH_CHECK();
 }

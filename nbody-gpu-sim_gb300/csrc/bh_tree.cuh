@@ -78,6 +78,7 @@ struct BHState {
   DevBuf<uint32_t> walk_ctr;  // next warp task of the walk
   DevBuf<int4> groups;        // group walk: first body, count, segment
   bool groups_ready = false;  // the last build emitted groups
+  int group_max = 32;           // largest group of the last build (32 or 64 bodies)
   DevBuf<char> group_ctr;     // group walk: GroupCounters
   DevBuf<int> group_ovf;      // group walk: stack overflow chunks
   int64_t n = 0;
@@ -100,9 +101,11 @@ struct SegView {
 };
 
 // Barnes-Hut group walk parameters (see the group walk below).
-constexpr int kGroupSize = 32;        // bodies per group (one per lane)
+constexpr int kGroupSize = 64;        // largest group (two bodies per lane above 32)
+constexpr int kGroupSmall = 32;       // groups of builds below kGroup64MinBodies bodies
+constexpr int64_t kGroup64MinBodies = 262144;  // from here on groups of up to 64 bodies
 constexpr int kGroupMergeMax = 1024;  // sibling subtrees merge only under parents this small
-constexpr int kGWarps = 8;            // warps (groups in flight) per block, 4 blocks per SM
+constexpr int kGWarps = 8;            // warps (groups in flight) per block
 constexpr int kGStack = 512;          // per-warp shared stack (nodes to test)
 constexpr int kGRing = 64;            // per-warp ring of pending list entries
 constexpr int kGSmallRun = 16;        // bucket / leaf bodies listed lane-parallel up to this
@@ -116,6 +119,12 @@ struct GroupCounters {
   uint32_t ovf;      // overflow chunks handed out
   uint32_t pad;
 };
+
+// Largest group of a build over n bodies (all segments together): groups of
+// up to 64 bodies halve the traversal per body and the list reads per
+// interaction, but give half as many warps, which only pays when the walk
+// has enough groups to fill the GPU.
+inline int bh_group_max(int64_t n) { return n >= kGroup64MinBodies ? kGroupSize : kGroupSmall; }
 
 // Centre of mass and cube of a node in one 256-bit load (read-only path),
 // as the register pairs (com x, y), (com z, mass), (centre x, y), (centre z, half).

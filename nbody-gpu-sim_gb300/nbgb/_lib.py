@@ -117,6 +117,7 @@ _SIGS = {
     "nbgb_init_params_default": (None, [C.POINTER(InitParams), C.c_int32]),
     "nbgb_selftest_wait_timeout": (C.c_int, [C.c_uint32, C.POINTER(C.c_uint32)]),
     "nbgb_selftest_group_walk_stack": (C.c_int, [C.c_int32]),
+    "nbgb_bh_group_size": (C.c_int32, [C.c_uint64]),
     "nbgb_init_particles_device": (C.c_int, [_pd, C.POINTER(InitParams), C.c_uint64, _vp]),
     "nbgb_bh_tree_stats": (C.c_int, [_vp, _i32p, _i32p]),
     "nbgb_bh_copy_sorted_keys": (C.c_int, [_vp, _vp, _vp, C.c_size_t]),

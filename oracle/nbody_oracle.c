@@ -592,10 +592,11 @@ int orc_bh_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* 
 
 /* Group walk (the library's NBGB_FLAG_GROUP_WALK; the reference has no
  * such walk -- it restates the same tree and opening quantities, see
- * orc_bh_forces above).  Groups: the root if it holds at most 32 bodies;
+ * orc_bh_forces above).  Groups: the root if it holds at most group_max
+ * bodies (32 or 64, the library's choice for the build's body count);
  * below a larger node, runs of consecutive children (octant order) holding
- * at most 32 bodies in total, merged only when the parent holds at most 1024
- * bodies; a child of more than 32 bodies ends the run.  The group's box is
+ * at most group_max bodies in total, merged only when the parent holds at
+ * most 1024 bodies; a child of more than group_max bodies ends the run.  The group's box is
  * its bounding box as a centre b = (lo + hi) * 0.5 and half sizes
  * max(hi - b, b - lo) * (1 + 2^-22).  Each group walks the tree once from the
  * root: a node of zero mass is skipped, a leaf adds its body, an internal
@@ -610,7 +611,7 @@ int orc_bh_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* 
  * zero-distance entry adds nothing.  Multi-body (depth-32) leaves are not
  * supported here (their bodies are not listed in the node records):
  * returns ORC_ERR_ARG. */
-#define ORC_GROUP 32
+#define ORC_GROUP 64
 #define ORC_GROUP_MERGE 1024
 
 typedef struct {
@@ -634,21 +635,21 @@ static void orc_subtree_bodies(const orc_node* nodes, int ni, int* out, int* nb,
     if (nd->children[c] >= 0) orc_subtree_bodies(nodes, nd->children[c], out, nb, cap, bad);
 }
 
-static void orc_group_bodies(const orc_node* nodes, int ni, int* out, int* nb, int* bad) {
-  orc_subtree_bodies(nodes, ni, out, nb, ORC_GROUP, bad);
+static void orc_group_bodies(const orc_node* nodes, int ni, int* out, int* nb, int cap, int* bad) {
+  orc_subtree_bodies(nodes, ni, out, nb, cap, bad);
 }
 
 int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const float* x,
                         const float* y, const float* z, const float* m, float theta, float G,
                         float eps, float* ax, float* ay, float* az, int32_t* interactions,
-                        int leaf_cap) {
-  if (num_nodes < 1) return ORC_ERR_ARG;
+                        int leaf_cap, int group_max) {
+  if (num_nodes < 1 || group_max < 1 || group_max > ORC_GROUP) return ORC_ERR_ARG;
   /* groups, by a pre-order pass over the nodes of more than ORC_GROUP bodies */
   orc_group* groups = (orc_group*)malloc(sizeof(orc_group) * (size_t)(n + 1));
   int* st = (int*)malloc(sizeof(int) * (size_t)(num_nodes + 8));
   int64_t ng = 0;
   int bad = 0, sp = 0;
-  if (nodes[0].particle_count <= ORC_GROUP) {
+  if (nodes[0].particle_count <= group_max) {
     groups[ng].nmem = 1;
     groups[ng++].mem[0] = 0;
   } else {
@@ -657,7 +658,7 @@ int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const f
   while (sp > 0) {
     const orc_node* nd = &nodes[st[--sp]];
     if (nd->is_leaf) {
-      bad = 1; /* a leaf of more than ORC_GROUP bodies */
+      bad = 1; /* a leaf of more than group_max bodies */
       continue;
     }
     int merge = nd->particle_count <= ORC_GROUP_MERGE, gn = 0;
@@ -665,10 +666,10 @@ int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const f
       int ch = nd->children[c];
       if (ch < 0) continue;
       int cc = nodes[ch].particle_count;
-      if (cc > ORC_GROUP) {
+      if (cc > group_max) {
         gn = 0;
         st[sp++] = ch;
-      } else if (gn && merge && gn + cc <= ORC_GROUP) {
+      } else if (gn && merge && gn + cc <= group_max) {
         groups[ng - 1].mem[groups[ng - 1].nmem++] = ch;
         gn += cc;
       } else {
@@ -683,7 +684,8 @@ int orc_bh_group_forces(const orc_node* nodes, int num_nodes, int64_t n, const f
 #pragma omp parallel for schedule(dynamic, 16) reduction(| : bad)
   for (int64_t g = 0; g < ng; g++) {
     int body[ORC_GROUP], nb = 0, gbad = 0;
-    for (int j = 0; j < groups[g].nmem; j++) orc_group_bodies(nodes, groups[g].mem[j], body, &nb, &gbad);
+    for (int j = 0; j < groups[g].nmem; j++)
+      orc_group_bodies(nodes, groups[g].mem[j], body, &nb, group_max, &gbad);
     if (gbad) {
       bad = 1;
       continue;

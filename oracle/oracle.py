@@ -74,7 +74,7 @@ class Oracle:
                                       C.c_void_p, C.c_int]
         lib.orc_bh_group_forces.argtypes = [C.c_void_p, C.c_int, _i64, _f32p, _f32p, _f32p,
                                             _f32p, _f, _f, _f, _f32p, _f32p, _f32p, C.c_void_p,
-                                            C.c_int]
+                                            C.c_int, C.c_int]
         lib.orc_hash_dims.argtypes = [_i64, _f32p, _f32p, _f32p, _f, _f32p, _f32p, _i32p,
                                       C.POINTER(C.c_int64)]
         lib.orc_cell_coords.argtypes = [_f, _f, _f, _f32p, _f, _i32p]
@@ -190,16 +190,18 @@ class Oracle:
             raise ValueError("oracle bucket walk: a bucket holds a multi-body leaf")
         return ax, ay, az, inter
 
-    def bh_group_forces(self, nodes, x, y, z, m, theta, G, eps, leaf_capacity=1):
+    def bh_group_forces(self, nodes, x, y, z, m, theta, G, eps, leaf_capacity=1, group_max=32):
         """Group walk over the whole system: (ax, ay, az, interactions); with
-        leaf_capacity > 1 opened buckets of at most that many bodies list them."""
+        leaf_capacity > 1 opened buckets of at most that many bodies list them;
+        group_max: the largest group (the library's choice for the body count)."""
         x, y, z, m = map(_f32, (x, y, z, m))
         nodes = np.ascontiguousarray(nodes, NODE_DTYPE)
         n = len(x)
         ax, ay, az = (np.zeros(n, np.float32) for _ in range(3))
         inter = np.zeros(n, np.int32)
         rc = self.lib.orc_bh_group_forces(nodes.ctypes.data, len(nodes), n, x, y, z, m, theta, G,
-                                          eps, ax, ay, az, inter.ctypes.data, leaf_capacity)
+                                          eps, ax, ay, az, inter.ctypes.data, leaf_capacity,
+                                          group_max)
         if rc != 0:
             raise ValueError("oracle group walk: multi-body leaves are not supported")
         return ax, ay, az, inter

@@ -70,3 +70,11 @@ def test_group_walk_stack_hook_validates(nb):
     assert lib.nbgb_selftest_group_walk_stack(63) == 1  # NBGB_ERR_INVALID_ARG
     assert lib.nbgb_selftest_group_walk_stack(513) == 1
     assert lib.nbgb_selftest_group_walk_stack(512) == 0  # the default
+
+
+def test_group_size_rule(nb):
+    """The group walk's largest group: 32 bodies below 262,144 bodies per
+    build, 64 from there on (host-only call)."""
+    f = nb.lib().nbgb_bh_group_size
+    assert [f(n) for n in (0, 1, 1000, 262143)] == [32] * 4
+    assert [f(n) for n in (262144, 1 << 20, 1 << 40)] == [64] * 3

@@ -42,6 +42,11 @@ def _bh(nb, s, theta=0.5, eps=0.01, leaf=1, count=True, G=1.0, group=False):
     return out
 
 
+def _gmax(nb, s):
+    """The largest group the library forms for this many bodies (32 or 64)."""
+    return int(nb.lib().nbgb_bh_group_size(len(s["x"])))
+
+
 def _oracle_tree(orc, s, max_nodes=None):
     bmin, bmax = orc.bbox(s["x"], s["y"], s["z"])
     keys, idx = orc.morton_keys(s["x"], s["y"], s["z"], bmin, bmax)
@@ -161,18 +166,21 @@ def _gen(nb, gen, n):
                                              ("two", 50000, 0.5, 0.01), ("cube", 30000, 0.5, 0.01),
                                              ("far", 6000, 0.5, 0.01), ("dense", 6000, 0.5, 0.01),
                                              ("plummer", 3000, 1.0, 0.01), ("plummer", 4000, 0.5, 0.0),
-                                             ("plummer", 3000, 2.0, 0.01), ("cube", 5000, 0.5, 5.0)])
+                                             ("plummer", 3000, 2.0, 0.01), ("cube", 5000, 0.5, 5.0),
+                                             ("two", 300000, 0.5, 0.01), ("plummer", 262144, 0.5, 0.0)])
 def test_group_walk_matches_oracle(nb, orc, gen, n, theta, eps):
     """Group walk: per-body list lengths (interactions) equal the oracle's
     group walk on the same tree -- same groups, same bounding boxes, same
     acceptance arithmetic -- and forces agree within 1e-5 (p99, vector
     relative; the list order differs).  eps = 0 runs the zero-softening
-    variant (zero-distance entries add nothing)."""
+    variant (zero-distance entries add nothing).  From 262,144 bodies on the
+    groups hold up to 64 bodies, two per lane."""
     s = _gen(nb, gen, n)
     _, _, nodes, _, merges = _oracle_tree(orc, s)
     assert merges == 0
     r = _bh(nb, s, theta=theta, eps=eps, group=True)
-    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], theta, 1.0, eps)
+    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], theta, 1.0, eps,
+                                           group_max=_gmax(nb, s))
     np.testing.assert_array_equal(r["inter"], oint)
     err = vec_rel_err(*r["acc"], ox, oy, oz)
     assert np.percentile(err, 99) <= 1e-5, np.percentile(err, 99)
@@ -213,7 +221,8 @@ def test_group_walk_spill_path(nb, orc, small_group_stack):
     s = nb.ics.plummer(n, seed=22)
     _, _, nodes, _, _ = _oracle_tree(orc, s)
     r = _bh(nb, s, theta=0.2, group=True)
-    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.2, 1.0, 0.01)
+    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.2, 1.0, 0.01,
+                                           group_max=_gmax(nb, s))
     np.testing.assert_array_equal(r["inter"], oint)
     assert np.percentile(vec_rel_err(*r["acc"], ox, oy, oz), 99) <= 1e-5
 
@@ -243,7 +252,7 @@ def test_group_walk_buckets_match_oracle(nb, orc, gen, n, theta, leaf):
     assert merges == 0
     r = _bh(nb, s, theta=theta, leaf=leaf, group=True)
     ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], theta, 1.0,
-                                           0.01, leaf)
+                                           0.01, leaf, group_max=_gmax(nb, s))
     np.testing.assert_array_equal(r["inter"], oint)
     err = vec_rel_err(*r["acc"], ox, oy, oz)
     assert np.percentile(err, 99) <= 1e-5, np.percentile(err, 99)
@@ -365,7 +374,9 @@ def test_full_size_two_plummer(nb, orc):
     # group walk on the same tree, forces within 1e-5 of it, and a lower
     # error against FP64 than the reference walk
     rg = _bh(nb, s, theta=0.5, group=True)
-    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.5, 1.0, 0.01)
+    assert _gmax(nb, s) == 64  # a build this large forms groups of up to 64 bodies
+    ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.5, 1.0, 0.01,
+                                           group_max=64)
     np.testing.assert_array_equal(rg["inter"], oint)
     assert np.percentile(vec_rel_err(*rg["acc"], ox, oy, oz), 99) <= 1e-5
     errg = vec_rel_err(*(a[t] for a in rg["acc"]), bx, by, bz)
@@ -375,7 +386,7 @@ def test_full_size_two_plummer(nb, orc):
     # median error <= 2e-3 and no worse than either reference-style walk
     rg8 = _bh(nb, s, theta=0.5, leaf=8, group=True)
     ox, oy, oz, oint = orc.bh_group_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.5, 1.0, 0.01,
-                                           8)
+                                           8, group_max=64)
     np.testing.assert_array_equal(rg8["inter"], oint)
     assert np.percentile(vec_rel_err(*rg8["acc"], ox, oy, oz), 99) <= 1e-5
     errg8 = vec_rel_err(*(a[t] for a in rg8["acc"]), bx, by, bz)

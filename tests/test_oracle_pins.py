@@ -255,7 +255,8 @@ def test_integrator_known_answers(orc):
     assert abs(orc.kinetic_energy([1.0, 0.0], [0.0, 2.0], [0.0, 0.0], [1.0, 2.0]) - 4.5) < 1e-12
 
 
-def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False, leaf_cap=1):
+def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False, leaf_cap=1,
+                   group_max=32):
     """Restatement of the group walk in Python (float32 operations one at a
     time; fma via an exact float64 product), pinning the C oracle's group
     rule and acceptance arithmetic.  With check_reference_test, every cell
@@ -263,9 +264,10 @@ def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False, leaf_
     (force_barnes_hut.cu:218-224: not containing the body, 4h^2 / (d^2 +
     eps^2) < theta^2) for every body of the group.  With leaf_cap > 1 an
     internal node of at most leaf_cap bodies that the group does not accept
-    lists its bodies instead of being opened."""
+    lists its bodies instead of being opened.  group_max: the largest group
+    (32 or 64)."""
     f = np.float32
-    G, MERGE = 32, 1024
+    G, MERGE = group_max, 1024
 
     def bodies(ni):
         nd = nodes[ni]
@@ -345,9 +347,12 @@ def _py_group_walk(nodes, x, y, z, theta, eps, check_reference_test=False, leaf_
     return np.array([counts[i] for i in range(len(x))])
 
 
-@pytest.mark.parametrize("n,theta,leaf", [(300, 0.5, 1), (700, 0.3, 1), (500, 1.0, 1),
-                                          (600, 0.5, 8), (400, 0.7, 4), (900, 0.5, 16)])
-def test_group_walk_oracle_matches_python_restatement(orc, n, theta, leaf):
+@pytest.mark.parametrize("n,theta,leaf,gmax", [(300, 0.5, 1, 32), (700, 0.3, 1, 32),
+                                               (500, 1.0, 1, 32), (600, 0.5, 8, 32),
+                                               (400, 0.7, 4, 32), (900, 0.5, 16, 32),
+                                               (700, 0.5, 1, 64), (900, 0.3, 1, 64),
+                                               (800, 0.5, 8, 64), (600, 1.0, 4, 64)])
+def test_group_walk_oracle_matches_python_restatement(orc, n, theta, leaf, gmax):
     import nbgb.ics as ics
     s = ics.plummer(n, seed=n)
     x, y, z, m = (np.asarray(s[k], np.float32) for k in ("x", "y", "z", "m"))
@@ -355,10 +360,10 @@ def test_group_walk_oracle_matches_python_restatement(orc, n, theta, leaf):
     _, si = orc.stable_sort(*orc.morton_keys(x, y, z, bmin, bmax))
     nodes, _, merges = orc.build_octree(x, y, z, m, si, bmin, bmax, max_nodes=64 * n + 64)
     assert merges == 0
-    _, _, _, inter = orc.bh_group_forces(nodes, x, y, z, m, theta, 1.0, 0.01, leaf)
+    _, _, _, inter = orc.bh_group_forces(nodes, x, y, z, m, theta, 1.0, 0.01, leaf, gmax)
     np.testing.assert_array_equal(inter, _py_group_walk(nodes, x, y, z, theta, 0.01,
                                                         check_reference_test=True,
-                                                        leaf_cap=leaf))
+                                                        leaf_cap=leaf, group_max=gmax))
     if leaf > 1:  # buckets only replace cells by finer entries: lists grow
-        _, _, _, inter1 = orc.bh_group_forces(nodes, x, y, z, m, theta, 1.0, 0.01, 1)
+        _, _, _, inter1 = orc.bh_group_forces(nodes, x, y, z, m, theta, 1.0, 0.01, 1, gmax)
         assert np.all(inter >= inter1)
