@@ -421,9 +421,11 @@ def gpu_arm(args, rank, world, local):
         w_achieved = 20.0 * bh_int / (walk_ms / 1e3) / 1e12 if walk_ms > 0 else None
         walk_share = (walk_ms / 1e3) / elapsed_s if elapsed_s > 0 else None
         direct_share = (dms / 1e3) / elapsed_s if elapsed_s > 0 else None
-        # DRAM bytes of one group-walk launch: ncu capture at N = 1,048,576
-        # (two Plummer spheres, 188.6 MB read + written), scaled by the bodies
-        walk_traffic = 188.6e6 * bh_bodies / 1048576 if bh_bodies else None
+        # DRAM bytes of the walk: ncu capture (dram__bytes_read.sum +
+        # dram__bytes_write.sum) of the group-walk launch of the first timed
+        # tick of this workload, 227.1 MB + 15.9 MB for 1,179,805 bodies
+        # walked, scaled by the bodies walked here
+        walk_traffic = 243.03e6 / 1179805 * bh_bodies if bh_bodies else None
         clocks = clk.summary()
         clocks["window"] = "timed ticks and the saturated end-to-end run"
         out = {
@@ -474,18 +476,19 @@ def gpu_arm(args, rank, world, local):
                 "bound": "fp32", "achieved": w_achieved, "peak": ffma_peak, "unit": "TFLOP/s",
                 "frac": (w_achieved / ffma_peak) if w_achieved else None,
                 "traffic": walk_traffic,
-                "traffic_source": "ncu dram__bytes_read+write of one group-walk launch at "
-                                  "N=1,048,576 (two Plummer spheres), scaled by the bodies "
-                                  "walked",
+                "traffic_source": "ncu dram__bytes_read+write of the group-walk launch of the "
+                                  "first timed tick of this workload (243.0 MB for 1,179,805 "
+                                  "bodies walked), scaled by the bodies walked",
                 "algorithmic_bytes": 64 * 1.5 * bh_bodies + 28 * bh_bodies if bh_bodies else None,
                 "peak_source": "measured in-process: FFMA chains on every SM "
                                "(nbgb_measure_fp32_peak); MEASURED_PEAKS.json has no FP32 figure",
                 "flops_per_interaction": 20, "share_of_tick": walk_share,
                 "walk_ms_per_tick": walk_ms / args.steps,
-                "note": "list evaluation in packed FP32x2 (6.3 FP32 instructions per "
-                        "entry) and a latency-bound traversal: FMA pipe 56 %, issue 65 %, "
-                        "shared-memory pipe 87 % (ncu, N=1M); interactions counted per "
-                        "lane (list length minus the body itself)",
+                "note": "list evaluation in packed FP32x2, two bodies per lane in groups "
+                        "of up to 64, and a latency-bound traversal: FMA pipe 66.5 %, issue "
+                        "63 %, warps active 35 % at 80 registers (ncu, N=1M two-Plummer); "
+                        "interactions counted per body (list length minus the body "
+                        "itself)",
                 "hbm_peak_gbs_measured": measured_peaks().get("hbm_gbs"),
             },
             "direct_kernel": {"kernel": "ens_direct_kernel (direct-sum work queue)",
