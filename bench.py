@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--ref-budget-s", type=float, default=120.0,
                     help="--impl reference: CPU seconds spread over warmup + steps")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--reference-walk", action="store_true",
+                    help="serve Barnes-Hut systems with the reference's per-target walk")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--case", choices=["direct", "bh", "bh8", "bhg", "bhg8", "hash", "integrate",
                                        "precision"], default=None,
@@ -327,7 +329,9 @@ def gpu_arm(args, rank, world, local):
     # --- batched, saturation --------------------------------------------------
     backlog = stream[: S + 256]
     states = {r["id"]: make_state(nbgb, r) for r in backlog}
-    ens = Ensemble(hbm_budget_bytes=64 << 30, max_resident=S, softening=EPS, theta=0.5)
+    walk = 0 if args.reference_walk else 1
+    ens = Ensemble(hbm_budget_bytes=64 << 30, max_resident=S, softening=EPS, theta=0.5,
+                   group_walk=walk)
     for r in backlog:
         ens.submit(states[r["id"]], r["steps"], DT)
     prime = 0
@@ -370,7 +374,7 @@ def gpu_arm(args, rank, world, local):
     tuned = s1["direct_config"]
     ens.close()
     # --- end to end at saturation: host arrays in, results read back ----------
-    e2e_rep = e2e_arm(nbgb, Ensemble, backlog, states, S, tuned, args.e2e_ticks, world)
+    e2e_rep = e2e_arm(nbgb, Ensemble, backlog, states, S, tuned, args.e2e_ticks, world, walk)
     clk.__exit__(None, None, None)
     del states
 
@@ -446,7 +450,9 @@ def gpu_arm(args, rank, world, local):
                                "group): median rel err <= 1e-3 vs FP64, below the reference "
                                "walk's (tests/test_bh_gpu.py, tests/test_direct_gpu.py); "
                                "measured on served systems: force_error_measured",
-                "bh_walk": "group walk (NBGB_FLAG_GROUP_WALK); the plain runs use the same",
+                "bh_walk": ("group walk (NBGB_FLAG_GROUP_WALK); the plain runs use the same"
+                            if walk else "the reference's per-target walk (--reference-walk) "
+                            "in the timed and end-to-end runs"),
                 "parallelism": f"replicas x{world} (request-stream shards)",
             },
             "force_error_measured": force_err,
@@ -557,7 +563,7 @@ def measured_force_error(nbgb) -> dict:
     return out
 
 
-def e2e_arm(nbgb, Ensemble, reqs, states, S, direct_config, ticks, world) -> dict:
+def e2e_arm(nbgb, Ensemble, reqs, states, S, direct_config, ticks, world, walk=1) -> dict:
     """The saturated serving loop through the public API: requests are
     submitted as host arrays (copied to the device at admission), the engine is
     ticked, and every finished request's state is polled back to the host
@@ -567,7 +573,7 @@ def e2e_arm(nbgb, Ensemble, reqs, states, S, direct_config, ticks, world) -> dic
     submits, polls and copies included, synchronised at both ends."""
     import itertools
     ens = Ensemble(hbm_budget_bytes=64 << 30, max_resident=S, softening=EPS, theta=0.5,
-                   direct_config=direct_config)
+                   direct_config=direct_config, group_walk=walk)
     feed = itertools.cycle(reqs)
     outstanding, h2d, d2h, results = 0, 0, 0, 0
 

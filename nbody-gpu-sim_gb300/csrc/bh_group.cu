@@ -104,24 +104,38 @@ __device__ __forceinline__ void group_eval(const float* ex, const float* ey, con
                        ring_pair(em, base + j), px, py, pz, e2, ax2, ay2, az2);
 }
 
-// Groups of 33..64 bodies: two targets per lane (bodies lane and lane + 32),
-// each pair of entries read from the ring once and added to both, which
-// halves the shared-memory reads per interaction.
-template <bool ZERO_EPS, bool FULL>
+// Groups of 33..64 bodies: each lane sums body `lane` over the whole list
+// and, for the h = count - 32 second bodies, lanes b, b + w, ... (w = 8, 16
+// or 32 >= h; REP2 = 32 / w replicas) sum second body b, replica r taking
+// pair r of every REP2 consecutive pairs, so no lane idles in the second
+// half when h <= 16.  The first body's pairs are read once for the whole
+// warp (broadcast); each replica reads its own pair for the second body.
+template <bool ZERO_EPS, bool FULL, int REP2>
 __device__ __forceinline__ void group_eval2(const float* ex, const float* ey, const float* ez,
-                                            const float* em, int base, int cnt, float4 pi,
-                                            float4 pj, float eps2, f2& ax2, f2& ay2, f2& az2,
-                                            f2& bx2, f2& by2, f2& bz2) {
+                                            const float* em, int base, int cnt, int r2,
+                                            float4 pi, float4 pj, float eps2, f2& ax2, f2& ay2,
+                                            f2& az2, f2& bx2, f2& by2, f2& bz2) {
   const f2 px = f2_make(pi.x, pi.x), py = f2_make(pi.y, pi.y), pz = f2_make(pi.z, pi.z);
   const f2 qx = f2_make(pj.x, pj.x), qy = f2_make(pj.y, pj.y), qz = f2_make(pj.z, pj.z);
   const f2 e2 = f2_make(eps2, eps2);
   const int jn = FULL ? 32 : cnt;
-#pragma unroll(FULL ? 8 : 1)
-  for (int j = 0; j < jn; j += 2) {
-    const f2 xj = ring_pair(ex, base + j), yj = ring_pair(ey, base + j),
-             zj = ring_pair(ez, base + j), m = ring_pair(em, base + j);
-    pair_add<ZERO_EPS>(xj, yj, zj, m, px, py, pz, e2, ax2, ay2, az2);
-    pair_add<ZERO_EPS>(xj, yj, zj, m, qx, qy, qz, e2, bx2, by2, bz2);
+#pragma unroll(FULL ? 8 / REP2 : 1)
+  for (int j = 0; j < jn; j += 2 * REP2) {
+    if (REP2 == 1) {
+      const f2 xj = ring_pair(ex, base + j), yj = ring_pair(ey, base + j),
+               zj = ring_pair(ez, base + j), m = ring_pair(em, base + j);
+      pair_add<ZERO_EPS>(xj, yj, zj, m, px, py, pz, e2, ax2, ay2, az2);
+      pair_add<ZERO_EPS>(xj, yj, zj, m, qx, qy, qz, e2, bx2, by2, bz2);
+    } else {
+#pragma unroll
+      for (int r = 0; r < REP2; ++r)
+        pair_add<ZERO_EPS>(ring_pair(ex, base + j + 2 * r), ring_pair(ey, base + j + 2 * r),
+                           ring_pair(ez, base + j + 2 * r), ring_pair(em, base + j + 2 * r), px,
+                           py, pz, e2, ax2, ay2, az2);
+      const int jb = base + j + 2 * r2;
+      pair_add<ZERO_EPS>(ring_pair(ex, jb), ring_pair(ey, jb), ring_pair(ez, jb),
+                         ring_pair(em, jb), qx, qy, qz, e2, bx2, by2, bz2);
+    }
   }
 }
 
@@ -155,13 +169,16 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
     if (t >= ngroups) break;
     const int4 g = a.groups[t];  // first, count, segment
     // a group of at most 8 (16) bodies gives each body 4 (2) lanes, each
-    // summing a share of the list: lane = replica * gw + body; a group of
-    // more than 32 bodies gives each lane two (lane and lane + 32)
+    // summing a share of the list: lane = replica * gw + body; in a group of
+    // more than 32 bodies every lane sums body `lane`, and its h - 32 second
+    // bodies get 32 / gw2 lanes each the same way (lane = replica * gw2 + b)
     const bool two = TWO && g.y > 32;
     const int gw = g.y <= 8 ? 8 : (g.y <= 16 ? 16 : 32);
     const int rep = 32 / gw, tl = lane & (gw - 1), rr = lane / gw;
-    const bool valid = tl < g.y, valid2 = two && lane + 32 < g.y;
-    const int k = g.x + (valid ? tl : 0), k2 = g.x + (valid2 ? lane + 32 : 0);
+    const int h2 = two ? g.y - 32 : 0, gw2 = h2 <= 8 ? 8 : (h2 <= 16 ? 16 : 32);
+    const int rep2 = 32 / gw2, tl2 = lane & (gw2 - 1), rr2 = lane / gw2;
+    const bool valid = tl < g.y, valid2 = two && tl2 < h2;
+    const int k = g.x + (valid ? tl : 0), k2 = g.x + (valid2 ? 32 + tl2 : 0);
     const float4 pi = a.spm[k];
     const float4 pj = two ? a.spm[k2] : pi;  // invalid second bodies repeat body 0
     {
@@ -188,12 +205,17 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
     // evaluates ring entries [base, base + cnt); full: a whole 32-entry chunk
     auto eval = [&](int base, int cnt, bool full_chunk) {
       if (two) {
-        if (full_chunk)
-          group_eval2<ZERO_EPS, true>(ex, ey, ez, em, base, 32, pi, pj, a.eps2, ax2, ay2, az2,
-                                      bx2, by2, bz2);
-        else
-          group_eval2<ZERO_EPS, false>(ex, ey, ez, em, base, cnt, pi, pj, a.eps2, ax2, ay2,
-                                       az2, bx2, by2, bz2);
+#define NBGB_EVAL2(F, R)                                                                        \
+  group_eval2<ZERO_EPS, F, R>(ex, ey, ez, em, base, F ? 32 : cnt, rr2, pi, pj, a.eps2, ax2, ay2, \
+                              az2, bx2, by2, bz2)
+        if (rep2 == 1) {
+          if (full_chunk) NBGB_EVAL2(true, 1); else NBGB_EVAL2(false, 1);
+        } else if (rep2 == 2) {
+          if (full_chunk) NBGB_EVAL2(true, 2); else NBGB_EVAL2(false, 2);
+        } else {
+          if (full_chunk) NBGB_EVAL2(true, 4); else NBGB_EVAL2(false, 4);
+        }
+#undef NBGB_EVAL2
       } else if (full_chunk && rep == 1) {
         group_eval<ZERO_EPS, true>(ex, ey, ez, em, base, 32, 0, 1, pi, a.eps2, ax2, ay2, az2);
       } else {
@@ -336,7 +358,7 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
         if (COUNT) {
           const uint32_t o = (uint32_t)(k - f), o2 = (uint32_t)(k2 - f);
           if (valid && rr == 0 && o < (uint32_t)c) selfmask |= 1ull << tl;
-          if (valid2 && o2 < (uint32_t)c) selfmask |= 1ull << (lane + 32);
+          if (valid2 && o2 < (uint32_t)c) selfmask |= 1ull << (32 + tl2);
         }
         for (int b = 0; b < c; b += 32) {
           const bool e = b + lane < c;
@@ -363,8 +385,9 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
       const float nan = __int_as_float(0x7fc00000);
       ax2 = ay2 = az2 = bx2 = by2 = bz2 = f2_make(nan, nan);
     } else {
-      // the rest of the list, padded to a multiple of 4 with massless entries
-      const int left = (int)(wr - rd), padded = (left + 3) & ~3;
+      // the rest of the list, padded to a multiple of 8 with massless entries
+      // (the evaluation takes up to four pairs at a time)
+      const int left = (int)(wr - rd), padded = (left + 7) & ~7;
       if (lane >= left && lane < padded) {
         const int slot = (int)((rd + lane) & (kGRing - 1));
         ex[slot] = 3.0e18f;
@@ -381,12 +404,18 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
       ay2 = f2_add(ay2, f2_shfl_xor(ay2, o));
       az2 = f2_add(az2, f2_shfl_xor(az2, o));
     }
+    if (two)
+      for (int o = gw2; o < 32; o <<= 1) {  // and the replicas of the second bodies
+        bx2 = f2_add(bx2, f2_shfl_xor(bx2, o));
+        by2 = f2_add(by2, f2_shfl_xor(by2, o));
+        bz2 = f2_add(bz2, f2_shfl_xor(bz2, o));
+      }
     if (COUNT)
       selfmask = (uint64_t)__reduce_or_sync(full, (uint32_t)selfmask) |
                  ((uint64_t)__reduce_or_sync(full, (uint32_t)(selfmask >> 32)) << 32);
     const int cnt_lane = (int)wr - (int)((selfmask >> tl) & 1u);
-    const int cnt_lane2 = (int)wr - (int)((selfmask >> (lane + 32)) & 1u);
-    const bool owner = valid && rr == 0;
+    const int cnt_lane2 = (int)wr - (int)((selfmask >> (32 + tl2)) & 1u);
+    const bool owner = valid && rr == 0, owner2 = valid2 && rr2 == 0;
     if (owner) {
       float sx0, sx1, sy0, sy1, sz0, sz1;
       f2_split(ax2, sx0, sx1);
@@ -398,7 +427,7 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
       a.az[i] = a.G * (sz0 + sz1);
       if (COUNT && a.counts) a.counts[i] = cnt_lane;
     }
-    if (valid2) {
+    if (owner2) {
       float sx0, sx1, sy0, sy1, sz0, sz1;
       f2_split(bx2, sx0, sx1);
       f2_split(by2, sy0, sy1);
@@ -413,7 +442,7 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
       const int own = CNT == 2 ? cnt_lane : (int)wr - (pi.w != 0.0f ? 1 : 0);
       const int own2 = CNT == 2 ? cnt_lane2 : (int)wr - (pj.w != 0.0f ? 1 : 0);
       unsigned long long c = (owner ? (unsigned long long)own : 0ull) +
-                             (valid2 ? (unsigned long long)own2 : 0ull);
+                             (owner2 ? (unsigned long long)own2 : 0ull);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(full, c, o);
       if (lane == 0) atomicAdd(a.inter_total, c);

@@ -24,7 +24,10 @@ NOT_READY = 6
 def default_config(**kw) -> EnsembleConfig:
     cfg = EnsembleConfig()
     _lib.lib().nbgb_ensemble_config_default(C.byref(cfg))
+    fields = {f[0] for f in cfg._fields_}
     for k, v in kw.items():
+        if k not in fields:  # a misspelt option must not be dropped silently
+            raise TypeError(f"unknown ensemble option {k!r}")
         setattr(cfg, k, v)
     return cfg
 

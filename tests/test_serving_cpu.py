@@ -3,6 +3,7 @@ mimics the ensemble's admission and retirement rules)."""
 from __future__ import annotations
 
 import numpy as np
+import pytest
 
 
 class FakeEngine:
@@ -76,3 +77,11 @@ def test_serve_stops_at_wall_limit(nb):
     rep = serve(FakeEngine(cap=2), reqs, lambda r: {"x": np.zeros(5, np.float32)},
                 time_scale=0.0, max_wall_s=0.2)
     assert rep.completed == 0 and rep.ticks > 0
+
+
+def test_ensemble_config_rejects_unknown_options(nb):
+    from nbgb.serving import default_config
+    cfg = default_config(group_walk=0, theta=0.7)
+    assert cfg.group_walk == 0 and abs(cfg.theta - 0.7) < 1e-7
+    with pytest.raises(TypeError, match="grup_walk"):
+        default_config(grup_walk=0)
