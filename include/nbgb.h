@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define NBGB_ABI_VERSION 1
+#define NBGB_ABI_VERSION 2
 
 /* Status codes.  The C++ adapter maps them to the reference's exceptions
  * (include/nbody/error_handling.hpp): INVALID_ARG -> ValidationException
@@ -88,6 +88,8 @@ typedef struct nbgb_params {
                              many bodies are summed body by body when opened (both
                              walks) */
   uint32_t flags;         /* NBGB_FLAG_* */
+  int32_t group_size;     /* group walk: largest group, 32 or 64 bodies; 0 (default) =
+                             by the body count (nbgb_bh_group_size) */
 } nbgb_params;
 
 /* Synchronize the calculator's stream at the end of each call and report any
@@ -105,9 +107,9 @@ typedef struct nbgb_params {
  * accelerations kept in FP64 (the full-FP64 reference variant; FP64
  * arithmetic runs at a small fraction of the FP32 rate on GB300). */
 #define NBGB_FLAG_FP64 0x8u
-/* Barnes-Hut group walk: the bodies of each small subtree (at most 32, or 64
- * in builds of 262,144 bodies or more -- nbgb_bh_group_size; consecutive
- * small sibling subtrees merged) share one interaction list; a
+/* Barnes-Hut group walk: the bodies of each small subtree (at most 32 or 64,
+ * nbgb_params.group_size; consecutive small sibling subtrees merged) share
+ * one interaction list; a
  * cell is accepted for the group when its cube does not touch the group's
  * bounding box and 4h^2 < theta^2 (d^2 + eps^2), d the distance from the
  * cell's centre of mass to the box.  Every accepted cell passes the
@@ -118,10 +120,12 @@ typedef struct nbgb_params {
  * the list instead of being opened (buckets). */
 #define NBGB_FLAG_GROUP_WALK 0x10u
 
-/* The largest group of the group walk in a tree build over `count` bodies
- * (all systems of one batched build together): 32, or 64 from 262,144
- * bodies on, where each lane of a group's warp sums two bodies.  Host-only;
- * no reference counterpart. */
+/* The largest group of the group walk that a calculator with group_size 0
+ * uses for `count` bodies: 32, or 64 from 262,144 bodies on (each lane of a
+ * group's warp then sums two bodies; below that, half as many groups would
+ * leave SMs idle).  The ensemble always uses 64, so that a system's result
+ * does not depend on what else is resident.  Host-only; no reference
+ * counterpart. */
 int32_t nbgb_bh_group_size(uint64_t count);
 
 void nbgb_params_default(nbgb_params* p);

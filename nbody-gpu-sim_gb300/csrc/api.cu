@@ -64,6 +64,8 @@ static void validate_params(nbgb_method m, const nbgb_params& p) {
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: Barnes-Hut theta must be between 0 and 2");
     if (p.leaf_capacity < 1 || p.leaf_capacity > 16)
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: leaf capacity must be between 1 and 16");
+    if (p.group_size != 0 && p.group_size != 32 && p.group_size != 64)
+      fail(NBGB_ERR_INVALID_ARG, "Validation Error: group size must be 0, 32 or 64");
   }
   if (m == NBGB_SPATIAL_HASH) {
     if (!(finite(p.cell_size) && p.cell_size > 0.f))
@@ -212,6 +214,7 @@ void nbgb_params_default(nbgb_params* p) {
   p->block_size = 256;     // cuda_block_size (:141)
   p->leaf_capacity = 1;    // reference tree: one body per leaf
   p->flags = NBGB_FLAG_SYNC | NBGB_FLAG_COMPENSATED;
+  p->group_size = 0;       // group walk: by the body count
 }
 
 const char* nbgb_last_error(void) { return g_last_error.c_str(); }

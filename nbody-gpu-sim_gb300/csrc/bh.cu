@@ -875,7 +875,8 @@ void bh_set_segments(BHState& h, const int64_t* off, const int64_t* n_per, int n
 
 // Builds the trees of all segments (positions and masses read from `pm` at
 // each segment's offset).
-void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups) {
+void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups,
+              int group_max) {
   const int64_t n = h.n;
   const int nseg = h.nseg;
   const size_t R = (size_t)h.reserve;  // per-body buffers are sized for the reserve
@@ -949,7 +950,7 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   internal_nodes_kernel<<<grid1d(h.cap), 256, 0, st>>>(ea);
   NBGB_LAUNCH_CHECK();
   if (groups) {
-    h.group_max = bh_group_max(n);
+    h.group_max = group_max > 0 ? group_max : bh_group_max(n);
     GroupSink gs{h.body, h.seg_of.ptr, grow(h.groups, R),
                  reinterpret_cast<GroupCounters*>(grow(h.group_ctr, sizeof(GroupCounters))),
                  h.group_max};
@@ -1053,7 +1054,7 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
   const bool sync = (c->params.flags & NBGB_FLAG_SYNC) != 0;
   if (!sync) bh_reserve_async(h);
   for (int attempt = 0; attempt < 2; ++attempt) {
-    bh_build(h, pm, st, err, (c->params.flags & NBGB_FLAG_GROUP_WALK) != 0);
+    bh_build(h, pm, st, err, (c->params.flags & NBGB_FLAG_GROUP_WALK) != 0, c->params.group_size);
     if (!sync) break;  // capacity overflow surfaces through the device error word
     // The node count is data dependent: read it back and regrow once if the
     // capacity was too small (the kernels skipped their work in that case).

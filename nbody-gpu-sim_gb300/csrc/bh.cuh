@@ -45,7 +45,10 @@ void bh_set_segments(BHState& h, const int64_t* off, const int64_t* n_per, int n
 void bh_reserve_async(BHState& h);
 // Trees of all segments (bit-identical, per segment, to the single-system tree);
 // `groups` also emits the group walk's groups.
-void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups);
+// groups: emit the group walk's groups, of at most group_max bodies (32 or
+// 64; 0 = by the body count, bh_group_max).
+void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups,
+              int group_max = 0);
 // Accelerations of all segments, written at each segment's offset into
 // ax/ay/az.  counts (per arena index) and inter_total (running sum) are
 // optional; err receives device error bits (group walk stack overflow).

@@ -43,6 +43,10 @@ namespace nbgb {
 
 constexpr int64_t kChunk = 256;  // arena granularity (== kDirTile)
 constexpr int kTimingRing = 8;   // direct-kernel event pairs in flight
+// The group walk's largest group in the batched build: fixed, so that a
+// system's lists (and results) do not depend on what else is resident; 64
+// pays off once the resident Barnes-Hut systems give the walk enough groups.
+constexpr int kEnsembleGroupMax = 64;
 
 struct DirectItem {
   int64_t off;  // arena offset of the system
@@ -527,12 +531,14 @@ static int64_t run_bh_pass(nbgb_ensemble* e) {
     NBGB_CUDA(cudaGraphLaunch(e->bh_exec, e->bh_stream));
     graph_kernels = e->bh_graph_kernels;
   } else if (!e->cfg.use_graphs || e->bh_stable < 1) {
-    bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr, e->cfg.group_walk != 0);
+    bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr, e->cfg.group_walk != 0,
+             kEnsembleGroupMax);
   } else {
     const int64_t l0 = t_launches;
     NBGB_CUDA(cudaStreamBeginCapture(e->bh_stream, cudaStreamCaptureModeThreadLocal));
     try {
-      bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr, e->cfg.group_walk != 0);
+      bh_build(*e->bh, e->pm.ptr, e->bh_stream, e->d_err.ptr, e->cfg.group_walk != 0,
+             kEnsembleGroupMax);
     } catch (...) {
       cudaGraph_t g = nullptr;
       cudaStreamEndCapture(e->bh_stream, &g);

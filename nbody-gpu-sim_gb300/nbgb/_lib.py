@@ -17,7 +17,7 @@ _HEADER = os.path.join(_build.REPO, "include", "nbgb.h")
 class Params(C.Structure):
     _fields_ = [("G", C.c_float), ("softening", C.c_float), ("theta", C.c_float),
                 ("cell_size", C.c_float), ("cutoff", C.c_float), ("block_size", C.c_int32),
-                ("leaf_capacity", C.c_int32), ("flags", C.c_uint32)]
+                ("leaf_capacity", C.c_int32), ("flags", C.c_uint32), ("group_size", C.c_int32)]
 
 
 class ParticleDataStruct(C.Structure):

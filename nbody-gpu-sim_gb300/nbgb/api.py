@@ -287,10 +287,14 @@ class BarnesHutCalculator(ForceCalculator):
     method = ForceMethod.BARNES_HUT
 
     def __init__(self, theta: float = 0.5, leaf_capacity: int = 1,
-                 params: Params | None = None, group_walk: bool = False) -> None:
+                 params: Params | None = None, group_walk: bool = False,
+                 group_size: int = 0) -> None:
+        """group_size: the group walk's largest group (32 or 64; 0 = by the
+        body count, as nbgb_bh_group_size)."""
         p = params if params is not None else default_params()
         p.theta = theta
         p.leaf_capacity = leaf_capacity
+        p.group_size = group_size
         if group_walk:
             p.flags |= FLAG_GROUP_WALK
         super().__init__(p)

@@ -31,18 +31,18 @@ def test_library_is_sm103a_only(nb):
 
 def test_abi_version_and_defaults(nb):
     lib = nb.lib()
-    assert lib.nbgb_abi_version() == 1
+    assert lib.nbgb_abi_version() == 2
     assert b"sm_103a" in lib.nbgb_version()
     p = nb.default_params()
     # SimulationConfig defaults (include/nbody/types.hpp:133-144)
     assert (p.G, p.softening, p.theta, p.cell_size, p.cutoff, p.block_size) == \
         (1.0, pytest.approx(0.1), 0.5, 2.0, 2.0, 256)
-    assert p.leaf_capacity == 1
+    assert p.leaf_capacity == 1 and p.group_size == 0
     assert p.flags & nb.FLAG_SYNC and p.flags & nb.FLAG_COMPENSATED
     # the drop-in calculator walks the tree as the reference does; the
     # serving engine defaults to the group walk
     assert not p.flags & nb.FLAG_GROUP_WALK
-    assert nb.BarnesHutCalculator.__init__.__defaults__[-1] is False  # group_walk
+    assert nb.BarnesHutCalculator.__init__.__defaults__[-2] is False  # group_walk
     from nbgb.serving import default_config
     cfg = default_config()
     assert cfg.group_walk == 1 and cfg.leaf_capacity == 1 and cfg.theta == 0.5

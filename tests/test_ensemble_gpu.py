@@ -61,6 +61,19 @@ def test_same_alone_and_in_mix_bitwise(nb):
             np.testing.assert_array_equal(alone[key][1][k], mixed[key][1][k])
 
 
+def test_group_walk_same_alone_and_beside_many_bodies(nb):
+    """The ensemble's groups have a fixed size, so a Barnes-Hut system's
+    group walk (and trajectory) is the same alone and beside 300,000 other
+    Barnes-Hut bodies (a single calculator would switch to groups of 64
+    bodies from 262,144 on)."""
+    sy = {"b20000": (nb.ics.plummer(20000, seed=15), 6)}
+    big = {f"big{i}": (nb.ics.plummer(60000, seed=40 + i), 6) for i in range(5)}
+    alone, _ = _run(nb, sy, direct_config=0, hbm_budget_bytes=4 << 30)
+    mixed, _ = _run(nb, {**sy, **big}, direct_config=0, hbm_budget_bytes=4 << 30)
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(alone["b20000"][1][k], mixed["b20000"][1][k])
+
+
 def test_same_alone_and_in_mix_autotuned(nb):
     sy = _systems(nb)
     mixed, stats = _run(nb, sy, hbm_budget_bytes=4 << 30)
@@ -98,7 +111,7 @@ def test_bh_system_matches_plain_bh(nb, group_walk):
     s = nb.ics.plummer(12000, seed=31)
     res, _ = _run(nb, {"b": (s, 30)}, direct_config=0, group_walk=group_walk)
     got = res["b"][1]
-    calc = nb.BarnesHutCalculator(0.5, group_walk=bool(group_walk))
+    calc = nb.BarnesHutCalculator(0.5, group_walk=bool(group_walk), group_size=64)
     calc.setSofteningParameter(0.01)
     sysm = nb.System(calc, s)
     sysm.step(1e-3, 30)
@@ -216,7 +229,8 @@ def test_batched_bh_bitwise_vs_calculator(nb, group_walk):
 
 
 def _calc_bh(nb, pos, m, theta=0.5, eps=0.01, group_walk=0):
-    calc = nb.BarnesHutCalculator(theta, group_walk=bool(group_walk))
+    # the ensemble's group walk always forms groups of up to 64 bodies
+    calc = nb.BarnesHutCalculator(theta, group_walk=bool(group_walk), group_size=64)
     calc.setSofteningParameter(eps)
     n = len(m)
     with nb.ScopedParticleData(n, {"pos_x": pos["x"], "pos_y": pos["y"], "pos_z": pos["z"],
