@@ -164,6 +164,38 @@ def link_reference_apps(lib_dir: str) -> dict[str, str] | None:
     return apps
 
 
+def link_adapter_runtime() -> str | None:
+    """The drop-in adapter (nbody-gpu-sim_gb300/adapter/nbody_adapter.cpp)
+    with the reference's error-handling and profiling sources, linked
+    against the fake C ABI of tests/adapter_runtime/fake_nbgb.c and driven
+    by tests/adapter_runtime/driver.cpp: a CPU check of the adapter's own
+    logic.  Outputs go to oracle/_ref/link/.  Returns the driver's path, or
+    None where the reference sources are absent."""
+    if not reference_available():
+        return None
+    root = _ref_root()
+    repo = os.path.dirname(HERE)
+    src = os.path.join(repo, "tests", "adapter_runtime")
+    out = os.path.join(REF_DIR, "link")
+    os.makedirs(out, exist_ok=True)
+    fake = os.path.join(out, "libnbgb_fake.so")
+    _run(["gcc", "-std=c11", "-O1", "-fPIC", "-shared", "-I", os.path.join(repo, "include"),
+          os.path.join(src, "fake_nbgb.c"), "-o", fake])
+    inc = ["-I", os.path.join(root, "include"), "-I", os.path.join(repo, "include"),
+           "-I", "/usr/local/cuda/include"]
+    defs = ["-DNDEBUG", "-DNBODY_WITH_CUDA=1", "-DNBODY_WITH_RENDERING=0", "-DNBODY_WITH_UI=0",
+            "-DNBODY_ENABLE_PROFILING=1"]
+    srcs = [os.path.join(repo, "nbody-gpu-sim_gb300", "adapter", "nbody_adapter.cpp"),
+            os.path.join(src, "driver.cpp"),
+            os.path.join(root, "src/utils/error_handling.cpp"),
+            os.path.join(root, "src/utils/performance_observability.cpp")]
+    exe = os.path.join(out, "adapter_runtime")
+    _run(["g++", "-std=c++17", "-O1"] + defs + inc + srcs +
+         ["-o", exe, "-L", out, "-lnbgb_fake", "-Wl,-rpath," + out,
+          "-L", "/usr/local/cuda/lib64", "-lcudart", "-lpthread"])
+    return exe
+
+
 if __name__ == "__main__":
     print(build_oracle(force=True))
     if "--ref" in sys.argv:
