@@ -575,6 +575,8 @@ __device__ __forceinline__ int arrive_acq_rel(int32_t* p) {
   return old;
 }
 
+constexpr int kComThreads = 64;
+
 // Leaves: mass/com as the reference's allocateLeaf + mergeParticleIntoLeaf
 // (force_barnes_hut.cu:355-389); then the last-arriving child of each node
 // computes that node from all its children in octant order (:514-538).
@@ -963,9 +965,10 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   h.groups_ready = groups;
   // one thread per node slot: a leaf thread carries centres of mass up the
   // tree, so slots are not chained per thread (one resident wave of threads
-  // striding over the slots was 0.3 ms per serving tick slower)
-  com_kernel<<<(unsigned)ceil_div(h.cap, 256), 256, 0, st>>>(nodes, spm, nst, n, h.cap, par, nch,
-                                                            vis);
+  // striding over the slots was 0.3 ms per serving tick slower); blocks of
+  // two warps, so that a block waiting for one long climb holds few slots
+  com_kernel<<<(unsigned)ceil_div(h.cap, kComThreads), kComThreads, 0, st>>>(nodes, spm, nst, n,
+                                                                          h.cap, par, nch, vis);
   NBGB_LAUNCH_CHECK();
 }
 
