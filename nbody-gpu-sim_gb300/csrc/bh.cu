@@ -403,6 +403,7 @@ struct EmitArgs {
   int32_t* seg_root;
   int32_t* seg_end;
   int32_t* seg_depth;
+  int32_t* leaf_of;  // per sorted body: the leaf node it starts, or -1
   uint32_t* err;
 };
 
@@ -442,6 +443,7 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
     idx += n_int;
     const bool leaf_start = first || (lp < kMaxDepth);
     int md = -1;
+    if (!leaf_start) a.leaf_of[k] = -1;
     if (leaf_start) {
       const int ld = min(kMaxDepth, max(lp, lk) + 1);
       float cx = b.center[0], cy = b.center[1], cz = b.center[2], h = b.half;
@@ -459,6 +461,7 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
       a.nodes[idx].info = make_int4((int)(idx + 1), (ld << 8) | 1, (int)k, (int)(e - k + 1));
       a.parent[idx] = -1;
       a.visit[idx] = 0;
+      a.leaf_of[k] = (int32_t)idx;
       // reference max_depth_: depth of the inserting body's last loop level
       md = (ld == kMaxDepth && e > k) ? kMaxDepth : ld - 1;
     }
@@ -583,13 +586,15 @@ constexpr int kComThreads = 64;
 __global__ void com_kernel(Node* __restrict__ nodes, const float4* __restrict__ spm,
                            const uint32_t* __restrict__ nstart, int64_t n, int64_t cap,
                            const int32_t* __restrict__ parent, const int32_t* __restrict__ nchild,
-                           int32_t* __restrict__ visit) {
+                           int32_t* __restrict__ visit, const int32_t* __restrict__ leaf_of) {
   const uint32_t total = nstart[n];
   if ((int64_t)total > cap) return;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
-       p += (int64_t)gridDim.x * blockDim.x) {
+  // one thread per sorted body; the bodies that start a leaf carry it
+  for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t p = leaf_of[k];
+    if (p < 0) continue;
     const int4 ip = nodes[p].info;
-    if (!(ip.y & 1)) continue;
     float4 b0 = spm[ip.z];
     float m = b0.w, cx = b0.x, cy = b0.y, cz = b0.z;
     for (int j = 1; j < ip.w; ++j) {
@@ -824,7 +829,8 @@ size_t bh_state_bytes(const BHState* p) {
          h.pidx.bytes() + h.pidx_alt.bytes() + h.sk.bytes() + h.sk_alt.bytes() + h.kseg.bytes() +
          h.hist.bytes() + h.scan_ws.bytes() + h.lcp.bytes() + h.ncnt.bytes() + h.nstart.bytes() +
          h.scalars.bytes() + h.nodes.bytes() +
-         h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() + h.spm.bytes() +
+         h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() +
+         h.leaf_of.bytes() + h.spm.bytes() +
          h.walk_ctr.bytes() + h.groups.bytes() + h.group_ctr.bytes() + h.group_ovf.bytes();
 }
 
@@ -945,8 +951,10 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   int32_t* par = grow(h.node_parent, (size_t)h.cap);
   int32_t* nch = grow(h.node_nchild, (size_t)h.cap);
   int32_t* vis = grow(h.node_visit, (size_t)h.cap);
+  int32_t* leaf_of = grow(h.leaf_of, R);
   EmitArgs ea{kseg, lcp, hi, lo, nst, spm, h.box.ptr, h.seg_base_p, n, h.cap, nodes, par,
-              vis, grow(h.seg_root, (size_t)nseg), grow(h.seg_end, (size_t)nseg), sdepth, err};
+              vis, grow(h.seg_root, (size_t)nseg), grow(h.seg_end, (size_t)nseg), sdepth,
+              leaf_of, err};
   emit_nodes_kernel<<<grid1d(n), 256, 0, st>>>(ea);
   NBGB_LAUNCH_CHECK();
   internal_nodes_kernel<<<grid1d(h.cap), 256, 0, st>>>(ea);
@@ -963,12 +971,13 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   }
   NBGB_LAUNCH_CHECK();
   h.groups_ready = groups;
-  // one thread per node slot: a leaf thread carries centres of mass up the
-  // tree, so slots are not chained per thread (one resident wave of threads
-  // striding over the slots was 0.3 ms per serving tick slower); blocks of
-  // two warps, so that a block waiting for one long climb holds few slots
-  com_kernel<<<(unsigned)ceil_div(h.cap, kComThreads), kComThreads, 0, st>>>(nodes, spm, nst, n,
-                                                                          h.cap, par, nch, vis);
+  // one thread per body that starts a leaf (found through leaf_of, so no
+  // thread idles on an unused node slot): it carries centres of mass up the
+  // tree, so bodies are not chained per thread (one resident wave of threads
+  // striding over the node slots was 0.3 ms per serving tick slower); blocks
+  // of two warps, so that a block waiting for one long climb holds few slots
+  com_kernel<<<(unsigned)ceil_div(std::max<int64_t>(n, 1), kComThreads), kComThreads, 0, st>>>(
+      nodes, spm, nst, n, h.cap, par, nch, vis, leaf_of);
   NBGB_LAUNCH_CHECK();
 }
 

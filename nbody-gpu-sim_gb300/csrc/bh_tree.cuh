@@ -74,6 +74,7 @@ struct BHState {
   HostPinned<uint32_t> h_scalars;
   DevBuf<Node> nodes;
   DevBuf<int32_t> node_parent, node_nchild, node_visit;
+  DevBuf<int32_t> leaf_of;  // per sorted body: the leaf it starts, or -1
   DevBuf<float4> spm;      // bodies in path order
   DevBuf<uint32_t> walk_ctr;  // next warp task of the walk
   DevBuf<int4> groups;        // group walk: first body, count, segment
