@@ -119,6 +119,15 @@ typedef struct nbgb_params {
  * node of at most that many bodies that is not accepted adds its bodies to
  * the list instead of being opened (buckets). */
 #define NBGB_FLAG_GROUP_WALK 0x10u
+/* Barnes-Hut: build the tree exactly as the reference's host build does,
+ * including its node budget of 2N (BarnesHutTree::buildTreeOnHost,
+ * force_barnes_hut.cu:391-543): once a split could overrun it, later bodies
+ * merge into existing leaves.  The default device build makes the canonical
+ * octree, which equals the reference's whenever the budget does not fire
+ * (in practice from about 100 bodies on).  With this flag the reference's
+ * insertion is replayed by one device thread: for systems of at most 65,536
+ * bodies, with the reference walk (no group walk, leaf_capacity 1). */
+#define NBGB_FLAG_REFERENCE_TREE 0x20u
 
 /* The largest group of the group walk that a calculator with group_size 0
  * uses for `count` bodies: 32, or 64 from 262,144 bodies on (each lane of a

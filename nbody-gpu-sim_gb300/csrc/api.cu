@@ -66,6 +66,11 @@ static void validate_params(nbgb_method m, const nbgb_params& p) {
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: leaf capacity must be between 1 and 16");
     if (p.group_size != 0 && p.group_size != 32 && p.group_size != 64)
       fail(NBGB_ERR_INVALID_ARG, "Validation Error: group size must be 0, 32 or 64");
+    if ((p.flags & NBGB_FLAG_REFERENCE_TREE) &&
+        ((p.flags & NBGB_FLAG_GROUP_WALK) || p.leaf_capacity != 1))
+      fail(NBGB_ERR_INVALID_ARG,
+           "Validation Error: the reference tree is walked with the reference walk only "
+           "(no group walk, leaf capacity 1)");
   }
   if (m == NBGB_SPATIAL_HASH) {
     if (!(finite(p.cell_size) && p.cell_size > 0.f))

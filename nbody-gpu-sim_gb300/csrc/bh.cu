@@ -578,6 +578,233 @@ __device__ __forceinline__ int arrive_acq_rel(int32_t* p) {
   return old;
 }
 
+// --------------------------------------------- reference-identical tree --
+// NBGB_FLAG_REFERENCE_TREE: the reference's host build
+// (BarnesHutTree::buildTreeOnHost, force_barnes_hut.cu:391-543) replayed by
+// one device thread -- insertion in Morton order, leaf splitting, the node
+// budget of 2N (a leaf is no longer split once node_count + 33 >= 2N, later
+// bodies merge into it, :449-453), depth-32 merges (:490-507), the
+// bottom-up centre of mass in descending node order (:514-538) -- with the
+// reference's float operations, then renumbered depth-first into the walk's
+// node records.  The canonical device build equals this tree whenever the
+// budget does not fire; for small systems (N below about 100) it can fire.
+constexpr int64_t kRefTreeMaxBodies = 65536;
+
+struct RefNode {
+  float cx, cy, cz, half;
+  float comx, comy, comz, mass;
+  int32_t child[8];
+  int32_t pidx;   // first inserted body (original index), -1 for internal nodes
+  int32_t count;  // bodies
+  int32_t leaf;
+  int32_t size;   // nodes in the subtree (renumbering)
+  int32_t minpos; // smallest sorted position of a body in the subtree
+};
+
+__device__ void ref_node_default(RefNode& r) {
+  r.cx = r.cy = r.cz = r.half = 0.f;
+  r.comx = r.comy = r.comz = r.mass = 0.f;
+  for (int c = 0; c < 8; ++c) r.child[c] = -1;
+  r.pidx = -1;
+  r.count = 0;
+  r.leaf = 1;
+  r.size = 1;
+  r.minpos = 0x7fffffff;
+}
+
+__device__ __forceinline__ int ref_octant(float x, float y, float z, const RefNode& r) {
+  return (x >= r.cx ? 1 : 0) | (y >= r.cy ? 2 : 0) | (z >= r.cz ? 4 : 0);
+}
+
+// mergeParticleIntoLeaf (:355-365)
+__device__ void ref_merge(RefNode& r, int32_t q, float4 p) {
+  const float t = __fadd_rn(r.mass, p.w);
+  r.comx = __fdiv_rn(__fadd_rn(__fmul_rn(r.comx, r.mass), __fmul_rn(p.x, p.w)), t);
+  r.comy = __fdiv_rn(__fadd_rn(__fmul_rn(r.comy, r.mass), __fmul_rn(p.y, p.w)), t);
+  r.comz = __fdiv_rn(__fadd_rn(__fmul_rn(r.comz, r.mass), __fmul_rn(p.z, p.w)), t);
+  r.mass = t;
+  r.count += 1;
+  if (r.pidx < 0) r.pidx = q;
+}
+
+// allocateLeaf (:368-389); false when the node array is full
+__device__ bool ref_alloc_leaf(RefNode* rn, int64_t max_nodes, int& count, int parent, int oct,
+                               int32_t q, float4 p) {
+  if ((int64_t)count >= max_nodes) return false;
+  const int ni = count++;
+  RefNode& pa = rn[parent];
+  pa.child[oct] = ni;
+  pa.leaf = 0;
+  const float hs = __fmul_rn(pa.half, 0.5f);
+  RefNode& c = rn[ni];
+  ref_node_default(c);
+  c.cx = __fadd_rn(pa.cx, (oct & 1) ? hs : -hs);
+  c.cy = __fadd_rn(pa.cy, (oct & 2) ? hs : -hs);
+  c.cz = __fadd_rn(pa.cz, (oct & 4) ? hs : -hs);
+  c.half = hs;
+  c.pidx = q;
+  c.count = 1;
+  c.mass = p.w;
+  c.comx = p.x;
+  c.comy = p.y;
+  c.comz = p.z;
+  return true;
+}
+
+struct RefTreeArgs {
+  const float4* pm;       // bodies by original index (one segment at offset 0)
+  const uint32_t* order;  // original indices in (Morton key, index) order
+  const uint32_t* body;   // sorted position -> original index
+  const BBox* box;
+  int64_t n;
+  int64_t cap;            // walk node records available
+  RefNode* rn;            // 2n reference nodes
+  int32_t* pos_of;        // original index -> sorted position
+  Node* nodes;
+  int32_t* parent;
+  uint32_t* nstart;       // nstart[n] = node count (the walk's capacity check)
+  uint32_t* scalars;      // [0] node count
+  int32_t* seg_root;
+  int32_t* seg_end;
+  int32_t* seg_depth;
+  uint32_t* err;
+};
+
+__global__ void ref_tree_kernel(RefTreeArgs a) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const int64_t n = a.n, max_nodes = 2 * n;  // the reference's max_nodes_ (:253)
+  const BBox b = *a.box;
+  RefNode* rn = a.rn;
+  ref_node_default(rn[0]);
+  rn[0].cx = b.center[0];
+  rn[0].cy = b.center[1];
+  rn[0].cz = b.center[2];
+  rn[0].half = b.half;
+  rn[0].leaf = 0;
+  rn[0].count = (int32_t)n;
+  int count = 1, max_depth = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    const int32_t q = (int32_t)a.order[i];
+    const float4 p = a.pm[q];
+    int cur = 0, depth = 0;
+    bool merged = false;
+    while (depth < kMaxDepth) {
+      RefNode& nd = rn[cur];
+      if (nd.leaf) {
+        if ((int64_t)count + kMaxDepth + 1 >= max_nodes) {  // the node budget
+          ref_merge(nd, q, p);
+          merged = true;
+          break;
+        }
+        const int32_t eq = nd.pidx;
+        const float4 ep = make_float4(nd.comx, nd.comy, nd.comz, nd.mass);
+        nd.leaf = 0;
+        nd.pidx = -1;
+        nd.count = 0;
+        nd.mass = 0.f;
+        nd.comx = nd.comy = nd.comz = 0.f;
+        const int eo = ref_octant(ep.x, ep.y, ep.z, nd);
+        if (nd.child[eo] < 0 && !ref_alloc_leaf(rn, max_nodes, count, cur, eo, eq, ep)) {
+          raise_error(a.err, kErrTreeCapacity);
+          return;
+        }
+      }
+      const int oct = ref_octant(p.x, p.y, p.z, rn[cur]);
+      const int ch = rn[cur].child[oct];
+      if (ch < 0) {
+        if (!ref_alloc_leaf(rn, max_nodes, count, cur, oct, q, p)) {
+          raise_error(a.err, kErrTreeCapacity);
+          return;
+        }
+        break;
+      }
+      cur = ch;
+      ++depth;
+    }
+    if (!merged && depth >= kMaxDepth) {  // coincident bodies: merge at depth 32
+      int leaf = cur;
+      while (!rn[leaf].leaf)
+        for (int c = 0; c < 8; ++c)
+          if (rn[leaf].child[c] >= 0) {
+            leaf = rn[leaf].child[c];
+            break;
+          }
+      ref_merge(rn[leaf], q, p);
+    }
+    max_depth = max(max_depth, depth);
+  }
+  if ((int64_t)count > a.cap) {
+    raise_error(a.err, kErrTreeCapacity);
+    return;
+  }
+  for (int64_t k = 0; k < n; ++k) a.pos_of[a.body[k]] = (int32_t)k;
+  // centre of mass bottom-up (children have larger indices than their
+  // parent), with subtree sizes and smallest body positions
+  for (int i = count - 1; i >= 0; --i) {
+    RefNode& nd = rn[i];
+    nd.size = 1;
+    if (nd.leaf) {
+      nd.minpos = a.pos_of[nd.pidx];
+      continue;
+    }
+    float tm = 0.f, sx = 0.f, sy = 0.f, sz = 0.f;
+    int32_t cnt = 0;
+    nd.minpos = 0x7fffffff;
+    for (int c = 0; c < 8; ++c) {
+      const int ci = nd.child[c];
+      if (ci < 0) continue;
+      const RefNode& ch = rn[ci];
+      tm = __fadd_rn(tm, ch.mass);
+      sx = __fadd_rn(sx, __fmul_rn(ch.comx, ch.mass));
+      sy = __fadd_rn(sy, __fmul_rn(ch.comy, ch.mass));
+      sz = __fadd_rn(sz, __fmul_rn(ch.comz, ch.mass));
+      cnt += ch.count;
+      nd.size += ch.size;
+      nd.minpos = min(nd.minpos, ch.minpos);
+    }
+    nd.mass = tm;
+    nd.count = cnt;
+    if (tm > 0.f) {
+      nd.comx = __fdiv_rn(sx, tm);
+      nd.comy = __fdiv_rn(sy, tm);
+      nd.comz = __fdiv_rn(sz, tm);
+    }
+  }
+  // depth-first renumbering (octant order), skip = next node after the
+  // subtree, next-sibling flags for the walk records
+  struct Item {
+    int ref, parent, depth, next;
+  };
+  Item stack[8 * (kMaxDepth + 2)];
+  int sp = 0, id = 0;
+  stack[sp++] = Item{0, -1, 0, 0};
+  while (sp > 0) {
+    const Item it = stack[--sp];
+    const RefNode& nd = rn[it.ref];
+    const int me = id++;
+    const int4 info = make_int4(me + nd.size, (it.depth << 8) | (nd.leaf ? 1 : 0),
+                                nd.leaf ? a.pos_of[nd.pidx] : nd.minpos, nd.count);
+    Node& o = a.nodes[me];
+    o.com = make_float4(nd.comx, nd.comy, nd.comz, nd.mass);
+    o.geom = make_float4(nd.cx, nd.cy, nd.cz, nd.half);
+    o.info = info;
+    o.walk = walk_record(info, nd.half, nd.mass, it.next != 0);
+    a.parent[me] = it.parent;
+    if (nd.leaf) continue;
+    int last = -1;
+    for (int c = 7; c >= 0; --c)
+      if (nd.child[c] >= 0) {
+        stack[sp++] = Item{nd.child[c], me, it.depth + 1, last >= 0 ? 1 : 0};
+        last = c;
+      }
+  }
+  a.nstart[n] = (uint32_t)count;
+  a.scalars[0] = (uint32_t)count;
+  a.seg_root[0] = 0;
+  a.seg_end[0] = count;
+  a.seg_depth[0] = max_depth;
+}
+
 constexpr int kComThreads = 64;
 
 // Leaves: mass/com as the reference's allocateLeaf + mergeParticleIntoLeaf
@@ -830,7 +1057,7 @@ size_t bh_state_bytes(const BHState* p) {
          h.hist.bytes() + h.scan_ws.bytes() + h.lcp.bytes() + h.ncnt.bytes() + h.nstart.bytes() +
          h.scalars.bytes() + h.nodes.bytes() +
          h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() +
-         h.leaf_of.bytes() + h.spm.bytes() +
+         h.leaf_of.bytes() + h.ref_nodes.bytes() + h.ref_pos.bytes() + h.spm.bytes() +
          h.walk_ctr.bytes() + h.groups.bytes() + h.group_ctr.bytes() + h.group_ovf.bytes();
 }
 
@@ -884,7 +1111,7 @@ void bh_set_segments(BHState& h, const int64_t* off, const int64_t* n_per, int n
 // Builds the trees of all segments (positions and masses read from `pm` at
 // each segment's offset).
 void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups,
-              int group_max) {
+              int group_max, bool ref_tree) {
   const int64_t n = h.n;
   const int nseg = h.nseg;
   const size_t R = (size_t)h.reserve;  // per-body buffers are sized for the reserve
@@ -933,6 +1160,43 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   tie_order_kernel<<<grid1d(n), 256, 0, st>>>(sv, n, kseg, hi, body, lo, spm);
   NBGB_LAUNCH_CHECK();
   h.keys_valid = false;  // Morton (key, index) pairs are produced on demand
+  if (ref_tree) {
+    if (nseg != 1 || n > kRefTreeMaxBodies)
+      fail(NBGB_ERR_INVALID_ARG,
+           "Validation Error: the reference tree takes one system of at most 65536 bodies");
+    // insertion order: the reference's Morton keys, stably sorted (:308-328)
+    uint32_t* mk = grow(h.mkeys, R);
+    uint32_t* mi = grow(h.midx, R);
+    uint32_t* mk2 = grow(h.mkeys_alt, R);
+    uint32_t* mi2 = grow(h.midx_alt, R);
+    morton_scatter_kernel<<<grid1d(n), 256, 0, st>>>(spm, body, n, h.box.ptr, mk, mi);
+    NBGB_LAUNCH_CHECK();
+    radix_sort_pairs<uint32_t>(mk, mk2, mi, mi2, n, 0, 32, hist, sws, st, &h.m_alt, err);
+    h.keys_valid = true;
+    const int64_t cap_min = 2 * n + 64;
+    if (h.cap < cap_min) h.cap = cap_min;
+    RefTreeArgs ra;
+    ra.pm = pm;
+    ra.order = h.m_alt ? mi2 : mi;
+    ra.body = body;
+    ra.box = h.box.ptr;
+    ra.n = n;
+    ra.cap = h.cap;
+    ra.rn = reinterpret_cast<RefNode*>(grow(h.ref_nodes, (size_t)(2 * n + 1) * sizeof(RefNode)));
+    ra.pos_of = grow(h.ref_pos, R);
+    ra.nodes = grow(h.nodes, (size_t)h.cap);
+    ra.parent = grow(h.node_parent, (size_t)h.cap);
+    ra.nstart = grow(h.nstart, R + 1);
+    ra.scalars = grow(h.scalars, 2);
+    ra.seg_root = grow(h.seg_root, 1);
+    ra.seg_end = grow(h.seg_end, 1);
+    ra.seg_depth = grow(h.seg_depth, 1);
+    ra.err = err;
+    ref_tree_kernel<<<1, 1, 0, st>>>(ra);
+    NBGB_LAUNCH_CHECK();
+    h.groups_ready = false;
+    return;
+  }
   // 3.-4. node counts, numbering, emission
   uint8_t* lcp = grow(h.lcp, R);
   uint32_t* cnt = grow(h.ncnt, R + 1);
@@ -1066,7 +1330,8 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
   const bool sync = (c->params.flags & NBGB_FLAG_SYNC) != 0;
   if (!sync) bh_reserve_async(h);
   for (int attempt = 0; attempt < 2; ++attempt) {
-    bh_build(h, pm, st, err, (c->params.flags & NBGB_FLAG_GROUP_WALK) != 0, c->params.group_size);
+    bh_build(h, pm, st, err, (c->params.flags & NBGB_FLAG_GROUP_WALK) != 0, c->params.group_size,
+             (c->params.flags & NBGB_FLAG_REFERENCE_TREE) != 0);
     if (!sync) break;  // capacity overflow surfaces through the device error word
     // The node count is data dependent: read it back and regrow once if the
     // capacity was too small (the kernels skipped their work in that case).

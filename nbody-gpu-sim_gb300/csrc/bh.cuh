@@ -47,8 +47,10 @@ void bh_reserve_async(BHState& h);
 // `groups` also emits the group walk's groups.
 // groups: emit the group walk's groups, of at most group_max bodies (32 or
 // 64; 0 = by the body count, bh_group_max).
+// ref_tree: the reference's insertion tree (node budget included) instead of
+// the canonical one; one segment of at most 65,536 bodies, no groups.
 void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups,
-              int group_max = 0);
+              int group_max = 0, bool ref_tree = false);
 // Accelerations of all segments, written at each segment's offset into
 // ax/ay/az.  counts (per arena index) and inter_total (running sum) are
 // optional; err receives device error bits (group walk stack overflow).

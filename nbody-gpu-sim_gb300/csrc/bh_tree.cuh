@@ -75,6 +75,8 @@ struct BHState {
   DevBuf<Node> nodes;
   DevBuf<int32_t> node_parent, node_nchild, node_visit;
   DevBuf<int32_t> leaf_of;  // per sorted body: the leaf it starts, or -1
+  DevBuf<char> ref_nodes;   // reference-identical build: the reference's node array
+  DevBuf<int32_t> ref_pos;  // reference-identical build: original index -> sorted position
   DevBuf<float4> spm;      // bodies in path order
   DevBuf<uint32_t> walk_ctr;  // next warp task of the walk
   DevBuf<int4> groups;        // group walk: first body, count, segment

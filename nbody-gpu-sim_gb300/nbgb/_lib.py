@@ -82,6 +82,7 @@ FLAG_COMPENSATED = 0x2
 FLAG_COUNT_INTERACTIONS = 0x4
 FLAG_FP64 = 0x8
 FLAG_GROUP_WALK = 0x10
+FLAG_REFERENCE_TREE = 0x20
 
 _vp = C.c_void_p
 _i32p = C.POINTER(C.c_int32)

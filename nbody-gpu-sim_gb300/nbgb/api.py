@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (FLAG_COMPENSATED, FLAG_COUNT_INTERACTIONS, FLAG_FP64, FLAG_GROUP_WALK,
-                   FLAG_SYNC, OctreeNode, Params)
+                   FLAG_REFERENCE_TREE, FLAG_SYNC, OctreeNode, Params)
 from ._lib import ParticleDataStruct
 
 FIELDS = ("pos_x", "pos_y", "pos_z", "vel_x", "vel_y", "vel_z", "acc_x", "acc_y", "acc_z",
@@ -488,5 +488,6 @@ __all__ = ["ForceMethod", "forceMethodToString", "ParticleData", "ParticleDataMa
            "Integrator", "System", "ValidationException", "ResourceException", "CudaException",
            "DeviceTimeout", "CapacityError", "NbodyError", "check", "default_params",
            "FLAG_SYNC", "FLAG_COMPENSATED", "FLAG_COUNT_INTERACTIONS", "FLAG_FP64", "FLAG_GROUP_WALK",
+           "FLAG_REFERENCE_TREE",
            "OctreeNode",
            "Params"]

@@ -22,13 +22,15 @@ from treeutil import compare
 pytestmark = pytest.mark.gpu
 
 
-def _bh(nb, s, theta=0.5, eps=0.01, leaf=1, count=True, G=1.0, group=False):
+def _bh(nb, s, theta=0.5, eps=0.01, leaf=1, count=True, G=1.0, group=False, ref_tree=False):
     calc = nb.BarnesHutCalculator(theta, leaf_capacity=leaf, group_walk=group)
     calc.setGravitationalConstant(G)
     calc.setSofteningParameter(eps)
-    if count:
-        calc.set_flags(nb.FLAG_SYNC | nb.FLAG_COUNT_INTERACTIONS | nb.FLAG_COMPENSATED |
-                       (nb.FLAG_GROUP_WALK if group else 0))
+    if count or ref_tree:
+        calc.set_flags(nb.FLAG_SYNC | nb.FLAG_COMPENSATED |
+                       (nb.FLAG_COUNT_INTERACTIONS if count else 0) |
+                       (nb.FLAG_GROUP_WALK if group else 0) |
+                       (nb.FLAG_REFERENCE_TREE if ref_tree else 0))
     n = len(s["x"])
     with nb.ScopedParticleData(n, {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"],
                                    "mass": s["m"]}) as p:
@@ -86,6 +88,67 @@ def test_tree_matches_reference_insertion(nb, orc, gen, n):
     np.testing.assert_array_equal(r["keys"][1], si)
     assert compare(r["nodes"], nodes) == []
     assert r["stats"] == (len(nodes), depth)
+
+
+@pytest.mark.parametrize("name", ["sph30", "sph100", "sph700", "uni500", "coincident16",
+                                  "collinear16"])
+def test_reference_tree_mode_matches_reference_golden(nb, golden, name):
+    """NBGB_FLAG_REFERENCE_TREE: node for node the tree the reference's own
+    host build made, including the cases where its 2N node budget merges
+    bodies into multi-body leaves (sph30: 9 bodies) and the degenerate
+    coincident / collinear inputs."""
+    s, keys, order, ref_nodes, ref_depth = _golden_tree(golden, name)
+    r = _bh(nb, s, ref_tree=True)
+    np.testing.assert_array_equal(r["keys"][1], order)
+    assert compare(r["nodes"], ref_nodes) == []
+    assert r["stats"] == (len(ref_nodes), ref_depth)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 5, 17, 30, 50, 64, 100, 300, 2000])
+def test_reference_tree_mode_matches_oracle_budget_tree_and_walk(nb, orc, n):
+    """The reference-identical tree against the oracle's restatement of the
+    reference build (2N budget), and the reference walk on it: interaction
+    counts bit-exact, forces within 1e-5 (p99) of the oracle walk."""
+    s = nb.ics.plummer(n, seed=40 + n)
+    _, _, nodes, depth, merges = _oracle_tree(orc, s)
+    r = _bh(nb, s, ref_tree=True)
+    assert compare(r["nodes"], nodes) == []
+    assert r["stats"] == (len(nodes), depth)
+    ox, oy, oz, oint = orc.bh_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.5, 1.0, 0.01)
+    np.testing.assert_array_equal(r["inter"], oint)
+    has = np.abs(ox) + np.abs(oy) + np.abs(oz) > 0
+    if has.any():
+        err = vec_rel_err(*(a[has] for a in r["acc"]), ox[has], oy[has], oz[has])
+        assert np.percentile(err, 99) <= 1e-5, np.percentile(err, 99)
+
+
+def test_reference_tree_mode_merges_where_the_budget_fires(nb, orc):
+    # the budget fires for some of these small systems, and the default
+    # (canonical) build then differs from the reference-identical one
+    fired = 0
+    for n in (20, 30, 40, 50):
+        s = nb.ics.plummer(n, seed=40 + n)
+        _, _, nodes, _, merges = _oracle_tree(orc, s)
+        if merges:
+            fired += 1
+            assert compare(_bh(nb, s)["nodes"], nodes) != []
+            assert compare(_bh(nb, s, ref_tree=True)["nodes"], nodes) == []
+    assert fired > 0
+
+
+def test_reference_tree_mode_limits(nb):
+    calc = nb.BarnesHutCalculator(0.5, group_walk=True)
+    with pytest.raises(nb.ValidationException):
+        calc.set_flags(nb.FLAG_SYNC | nb.FLAG_GROUP_WALK | nb.FLAG_REFERENCE_TREE)
+    calc.close()
+    big = nb.ics.plummer(65537, seed=4)
+    calc = nb.BarnesHutCalculator(0.5)
+    calc.set_flags(nb.FLAG_SYNC | nb.FLAG_REFERENCE_TREE)
+    with nb.ScopedParticleData(65537, {"pos_x": big["x"], "pos_y": big["y"], "pos_z": big["z"],
+                                       "mass": big["m"]}) as p:
+        with pytest.raises(nb.ValidationException, match="65536"):
+            calc.computeForces(p.device)
+    calc.close()
 
 
 def test_keys_with_duplicates_are_stable(nb, orc):

@@ -84,6 +84,38 @@ def test_grid_and_neighbours_bit_exact(nb, orc, n):
         assert np.all(ax[~has] == 0.0)
 
 
+@pytest.mark.parametrize("clump", [40, 65, 3000])
+def test_crowded_cells_match_oracle(nb, orc, clump):
+    """A uniform cube plus a clump of `clump` bodies inside one cell (cells of
+    very different sizes side by side): neighbour counts bit-exact, forces
+    within the file's tolerance."""
+    s = _cube(20000, seed=11)
+    rng = np.random.default_rng(12)
+    for k in ("x", "y", "z"):  # inside the cell [6, 8) of every axis
+        s[k][:clump] = (6.2 + rng.random(clump) * 1.5).astype(np.float32)
+    (ax, ay, az), cells, nbrs = _run(nb, s)
+    sizes = cells["cell_end"] - cells["cell_start"]
+    assert sizes.max() >= clump
+    g = orc.hash_build(s["x"], s["y"], s["z"], 2.0)
+    ox, oy, oz, onb = orc.hash_forces(g, s["x"], s["y"], s["z"], s["m"], 2.0, 1.0, 0.01)
+    np.testing.assert_array_equal(nbrs, onb)
+    has = onb > 0
+    err = vec_rel_err(ax[has], ay[has], az[has], ox[has], oy[has], oz[has])
+    assert np.percentile(err, 99) <= 1e-5 and err.max() <= 1e-3
+
+
+def test_all_bodies_in_one_cell(nb, orc):
+    # a cell larger than the system (as in a direct sum with a cutoff)
+    s = _cube(3000, seed=13)
+    (ax, ay, az), cells, nbrs = _run(nb, s, cell=1e3, cutoff=1e3)
+    assert cells["total_cells"] == 8 and (cells["cell_end"] - cells["cell_start"]).max() == 3000
+    g = orc.hash_build(s["x"], s["y"], s["z"], 1e3)
+    ox, oy, oz, onb = orc.hash_forces(g, s["x"], s["y"], s["z"], s["m"], 1e3, 1.0, 0.01)
+    np.testing.assert_array_equal(nbrs, onb)
+    err = vec_rel_err(ax, ay, az, ox, oy, oz)
+    assert np.percentile(err, 99) <= 1e-5 and err.max() <= 1e-3
+
+
 def test_every_particle_in_exactly_one_cell(nb):
     # tests/test_spatial_hash.cpp:133-167 (several cell sizes)
     rng = np.random.default_rng(0)
