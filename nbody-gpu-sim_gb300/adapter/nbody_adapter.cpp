@@ -201,9 +201,20 @@ BarnesHutTree::BarnesHutTree(size_t max_particles)
 
 BarnesHutTree::~BarnesHutTree() { release(this); }
 
+namespace {
+// The tree the reference's tests inspect: its own insertion tree (2N node
+// budget included) up to the reference-tree limit, the canonical device
+// tree above it (the two agree whenever the budget does not fire).
+nbgb_params tree_params(size_t count, float G = 1.0f, float eps = 0.1f) {
+  nbgb_params p = params_of(G, eps);
+  if (count <= 65536) p.flags |= NBGB_FLAG_REFERENCE_TREE;
+  return p;
+}
+}  // namespace
+
 void BarnesHutTree::build(const ParticleData* d_particles) {
   NBODY_PROFILE_SCOPE("barnes_hut.build");
-  nbgb_calculator* c = handle(this, NBGB_BARNES_HUT, params_of(1.0f, 0.1f));
+  nbgb_calculator* c = handle(this, NBGB_BARNES_HUT, tree_params(d_particles->count));
   build_into_scratch(c, d_particles);
   int32_t nc = 0, md = 0;
   check(nbgb_bh_tree_stats(c, &nc, &md));
@@ -212,13 +223,13 @@ void BarnesHutTree::build(const ParticleData* d_particles) {
 }
 
 void BarnesHutTree::computeForces(ParticleData* d_particles, float theta, float G, float eps) {
-  nbgb_params p = params_of(G, eps);
+  nbgb_params p = tree_params(d_particles->count, G, eps);
   p.theta = theta;
   check(nbgb_compute_forces(handle(this, NBGB_BARNES_HUT, p), view(d_particles)));
 }
 
 void BarnesHutTree::copyNodesToHost() {
-  nbgb_calculator* c = handle(this, NBGB_BARNES_HUT, params_of(1.0f, 0.1f));
+  nbgb_calculator* c = handle(this, NBGB_BARNES_HUT, tree_params(max_particles_));
   h_nodes_.resize((size_t)std::max(node_count_, 1));
   check(nbgb_bh_copy_nodes(c, reinterpret_cast<nbgb_octree_node*>(h_nodes_.data()),
                            h_nodes_.size()));

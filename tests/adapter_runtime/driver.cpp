@@ -9,6 +9,7 @@
 #include <stdexcept>
 #include <string>
 
+#include "nbody/barnes_hut_tree.hpp"
 #include "nbody/error_handling.hpp"
 #include "nbody/force_calculator.hpp"
 #include "nbody/integrator.hpp"
@@ -71,6 +72,18 @@ int main() {
   b->computeForces(&d);
   b->~BarnesHutCalculator();
   show("bh_lifecycle");
+
+  // 1b. the tree the reference's tests inspect is the reference's own tree
+  //     (the build's scratch allocation needs a device, which a CPU run does
+  //     not have: only the calculator it asked for is checked)
+  {
+    nbody::BarnesHutTree tree(4);
+    try {
+      tree.build(&d);
+    } catch (const std::exception&) {
+    }
+  }
+  show("tree_build");
 
   // 2. direct calculators share one library calculator
   {

@@ -70,14 +70,16 @@ void nbgb_params_default(nbgb_params* p) {
 
 nbgb_status nbgb_calculator_create(nbgb_method method, const nbgb_params* params,
                                    nbgb_calculator** out) {
-  (void)params;
   nbgb_status s = result();
   if (s != NBGB_OK) return s;
   nbgb_calculator* c = (nbgb_calculator*)malloc(sizeof *c);
   c->id = g_next_id++;
   c->method = (int)method;
   *out = c;
-  note("create:%d:%d", c->method, c->id);
+  if (params->flags & NBGB_FLAG_REFERENCE_TREE)
+    note("create:%d:%d:reftree", c->method, c->id);
+  else
+    note("create:%d:%d", c->method, c->id);
   return s;
 }
 

@@ -40,8 +40,14 @@ def test_one_calculator_per_object_released_with_it(lines):
                                      "create:1:2 compute:2:4 destroy:2")
 
 
+def test_tree_inspection_uses_the_reference_tree(lines):
+    # BarnesHutTree (the class the reference's tests inspect) asks for the
+    # reference's own insertion tree (NBGB_FLAG_REFERENCE_TREE)
+    assert lines["tree_build"] == "create:1:3:reftree destroy:3"
+
+
 def test_direct_calculators_share_one_library_calculator(lines):
-    assert lines["direct_shared"] == "create:0:3 compute:3:4 set_params:3 compute:3:4"
+    assert lines["direct_shared"] == "create:0:4 compute:4:4 set_params:4 compute:4:4"
 
 
 def test_status_codes_map_to_reference_exceptions(lines):
@@ -56,14 +62,14 @@ def test_status_codes_map_to_reference_exceptions(lines):
 
 def test_integrate_keeps_fp64_state_and_releases_it(lines):
     # kick-drift, the calculator (created at its first use), kick
-    assert lines["integrate_fp64"] == ("kick_drift:4 create:1:5 compute:5:4 kick:4 "
-                                       "kick_drift:4 set_params:5 compute:5:4 kick:4")
+    assert lines["integrate_fp64"] == ("kick_drift:4 create:1:6 compute:6:4 kick:4 "
+                                       "kick_drift:4 set_params:6 compute:6:4 kick:4")
     # NBGB_FP32_VERLET=1: the reference's three FP32 kernels around the forces
-    assert lines["integrate_fp32"] == ("store_old update_positions set_params:5 compute:5:4 "
+    assert lines["integrate_fp32"] == ("store_old update_positions set_params:6 compute:6:4 "
                                        "update_velocities")
     assert lines["energy"] == "-0.500"
     assert lines["integrate_invalid"] == \
         "ValidationException|Validation Error: Time step must be positive and finite"
     # the calculator goes first (declared last), then the integrator releases
     # the FP64 state of the ParticleData it integrated
-    assert lines["integrator_released"] == "destroy:5 release:4"
+    assert lines["integrator_released"] == "destroy:6 release:4"
