@@ -427,9 +427,9 @@ def gpu_arm(args, rank, world, local):
         direct_share = (dms / 1e3) / elapsed_s if elapsed_s > 0 else None
         # DRAM bytes of the walk: ncu capture (dram__bytes_read.sum +
         # dram__bytes_write.sum) of the group-walk launch of the first timed
-        # tick of this workload, 227.1 MB + 15.9 MB for 1,179,805 bodies
+        # tick of this workload, 216.6 MB + 19.8 MB for 1,179,805 bodies
         # walked, scaled by the bodies walked here
-        walk_traffic = 243.03e6 / 1179805 * bh_bodies if bh_bodies else None
+        walk_traffic = 236.43e6 / 1179805 * bh_bodies if bh_bodies else None
         clocks = clk.summary()
         clocks["window"] = "timed ticks and the saturated end-to-end run"
         out = {
@@ -483,7 +483,7 @@ def gpu_arm(args, rank, world, local):
                 "frac": (w_achieved / ffma_peak) if w_achieved else None,
                 "traffic": walk_traffic,
                 "traffic_source": "ncu dram__bytes_read+write of the group-walk launch of the "
-                                  "first timed tick of this workload (243.0 MB for 1,179,805 "
+                                  "first timed tick of this workload (236.4 MB for 1,179,805 "
                                   "bodies walked), scaled by the bodies walked",
                 "algorithmic_bytes": 64 * 1.5 * bh_bodies + 28 * bh_bodies if bh_bodies else None,
                 "peak_source": "measured in-process: FFMA chains on every SM "
@@ -491,8 +491,8 @@ def gpu_arm(args, rank, world, local):
                 "flops_per_interaction": 20, "share_of_tick": walk_share,
                 "walk_ms_per_tick": walk_ms / args.steps,
                 "note": "list evaluation in packed FP32x2, two bodies per lane in groups "
-                        "of up to 64, and a latency-bound traversal: FMA pipe 66.5 %, issue "
-                        "63 %, warps active 35 % at 80 registers (ncu, N=1M two-Plummer); "
+                        "of up to 64, and a latency-bound traversal: FMA pipe 64 %, issue "
+                        "65 %, warps active 35 % at 80 registers (ncu, N=1M two-Plummer); "
                         "interactions counted per body (list length minus the body "
                         "itself)",
                 "hbm_peak_gbs_measured": measured_peaks().get("hbm_gbs"),

@@ -125,8 +125,11 @@ typedef struct nbgb_params {
  * merge into existing leaves.  The default device build makes the canonical
  * octree, which equals the reference's whenever the budget does not fire
  * (in practice from about 100 bodies on).  With this flag the reference's
- * insertion is replayed by one device thread: for systems of at most 65,536
- * bodies, with the reference walk (no group walk, leaf_capacity 1). */
+ * insertion is replayed by one device thread where the trees can differ --
+ * with NBGB_FLAG_SYNC only when the canonical tree has at least 2N - 33
+ * nodes (otherwise it is the reference's tree), without it always -- for
+ * systems of at most 65,536 bodies, with the reference walk (no group walk,
+ * leaf_capacity 1).  The drop-in adapter sets it. */
 #define NBGB_FLAG_REFERENCE_TREE 0x20u
 
 /* The largest group of the group walk that a calculator with group_size 0

@@ -128,6 +128,9 @@ void BarnesHutCalculator::computeForces(ParticleData* d_particles) {
   NBODY_PROFILE_SCOPE("barnes_hut.build");
   nbgb_params p = params_of(G_, softening_eps_);
   p.theta = theta_;
+  // the reference's own tree wherever it differs from the canonical one
+  // (synchronous calls check the node count; only small systems pay)
+  if (d_particles->count <= 65536) p.flags |= NBGB_FLAG_REFERENCE_TREE;
   check(nbgb_compute_forces(handle(this, NBGB_BARNES_HUT, p), view(d_particles)));
 }
 

@@ -1328,17 +1328,28 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
     bh_set_segments(h, &off, &n, 1, st, nullptr);
   }
   const bool sync = (c->params.flags & NBGB_FLAG_SYNC) != 0;
+  const bool ref_tree = (c->params.flags & NBGB_FLAG_REFERENCE_TREE) != 0;
+  const bool groups = (c->params.flags & NBGB_FLAG_GROUP_WALK) != 0;
   if (!sync) bh_reserve_async(h);
   for (int attempt = 0; attempt < 2; ++attempt) {
-    bh_build(h, pm, st, err, (c->params.flags & NBGB_FLAG_GROUP_WALK) != 0, c->params.group_size,
-             (c->params.flags & NBGB_FLAG_REFERENCE_TREE) != 0);
+    // asynchronously the reference's tree is always replayed; synchronously
+    // the canonical tree is built first and replaced only where it can differ
+    bh_build(h, pm, st, err, groups, c->params.group_size, ref_tree && !sync);
     if (!sync) break;  // capacity overflow surfaces through the device error word
     // The node count is data dependent: read it back and regrow once if the
     // capacity was too small (the kernels skipped their work in that case).
     uint32_t* hs = h.h_scalars.ensure(2);
     NBGB_CUDA(cudaMemcpyAsync(hs, h.scalars.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     NBGB_CUDA(cudaStreamSynchronize(st));
-    if ((int64_t)hs[0] <= h.cap) break;
+    if ((int64_t)hs[0] <= h.cap) {
+      // The reference stops splitting once node_count + 33 >= 2N.  Its node
+      // count only grows during the insertion and ends at the canonical
+      // count when the budget never fires, so a canonical count below
+      // 2N - 33 proves that it never fires and the trees are the same.
+      if (ref_tree && (int64_t)hs[0] + kMaxDepth + 1 >= 2 * n)
+        bh_build(h, pm, st, err, groups, c->params.group_size, true);
+      break;
+    }
     NBGB_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
     h.cap = (int64_t)hs[0] + (int64_t)hs[0] / 8 + 64;
   }

@@ -36,8 +36,9 @@ def lines():
 def test_one_calculator_per_object_released_with_it(lines):
     # create (method 1 = Barnes-Hut, handle 1), reuse with new parameters,
     # destroy; a new object in the same storage gets a new calculator
-    assert lines["bh_lifecycle"] == ("create:1:1 compute:1:4 set_params:1 compute:1:4 destroy:1 "
-                                     "create:1:2 compute:2:4 destroy:2")
+    # (the reference tree flag: the reference's own tree wherever it differs)
+    assert lines["bh_lifecycle"] == ("create:1:1:reftree compute:1:4 set_params:1 compute:1:4 "
+                                     "destroy:1 create:1:2:reftree compute:2:4 destroy:2")
 
 
 def test_tree_inspection_uses_the_reference_tree(lines):
@@ -62,7 +63,7 @@ def test_status_codes_map_to_reference_exceptions(lines):
 
 def test_integrate_keeps_fp64_state_and_releases_it(lines):
     # kick-drift, the calculator (created at its first use), kick
-    assert lines["integrate_fp64"] == ("kick_drift:4 create:1:6 compute:6:4 kick:4 "
+    assert lines["integrate_fp64"] == ("kick_drift:4 create:1:6:reftree compute:6:4 kick:4 "
                                        "kick_drift:4 set_params:6 compute:6:4 kick:4")
     # NBGB_FP32_VERLET=1: the reference's three FP32 kernels around the forces
     assert lines["integrate_fp32"] == ("store_old update_positions set_params:6 compute:6:4 "

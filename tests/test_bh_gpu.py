@@ -136,6 +136,27 @@ def test_reference_tree_mode_merges_where_the_budget_fires(nb, orc):
     assert fired > 0
 
 
+@pytest.mark.parametrize("n", [30, 2000])
+def test_reference_tree_mode_asynchronous(nb, orc, n):
+    # without NBGB_FLAG_SYNC the reference's insertion is always replayed
+    s = nb.ics.plummer(n, seed=40 + n)
+    _, _, nodes, depth, _ = _oracle_tree(orc, s)
+    calc = nb.BarnesHutCalculator(0.5)
+    calc.setSofteningParameter(0.01)
+    calc.set_flags(nb.FLAG_COMPENSATED | nb.FLAG_REFERENCE_TREE)
+    with nb.ScopedParticleData(n, {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"],
+                                   "mass": s["m"]}) as p:
+        calc.computeForces(p.device)
+        calc.synchronize()
+        p.download()
+    assert compare(calc.nodes(), nodes) == []
+    assert calc.tree_stats() == (len(nodes), depth)
+    ox, oy, oz, _ = orc.bh_forces(nodes, s["x"], s["y"], s["z"], s["m"], 0.5, 1.0, 0.01)
+    err = vec_rel_err(p.host["acc_x"], p.host["acc_y"], p.host["acc_z"], ox, oy, oz)
+    assert np.percentile(err, 99) <= 1e-5
+    calc.close()
+
+
 def test_reference_tree_mode_limits(nb):
     calc = nb.BarnesHutCalculator(0.5, group_walk=True)
     with pytest.raises(nb.ValidationException):
