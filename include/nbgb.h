@@ -131,6 +131,14 @@ typedef struct nbgb_params {
  * systems of at most 65,536 bodies, with the reference walk (no group walk,
  * leaf_capacity 1).  The drop-in adapter sets it. */
 #define NBGB_FLAG_REFERENCE_TREE 0x20u
+/* Record the device time of each stage of every force evaluation (CUDA
+ * events on the calculator's stream) for nbgb_calculator_stage_times.
+ * Stages: direct.forces; barnes_hut.bounds, .keys, .sort, .order, .nodes,
+ * .com, .walk (.reference_tree with NBGB_FLAG_REFERENCE_TREE);
+ * spatial_hash.bounds, .assign, .sort, .cells, .forces.  The SURVEY-style
+ * counterpart of the reference's NBODY_PROFILE_SCOPE phases
+ * (performance_observability.hpp:70-78), measured on the device. */
+#define NBGB_FLAG_STAGE_TIMINGS 0x40u
 
 /* The largest group of the group walk that a calculator with group_size 0
  * uses for `count` bodies: 32, or 64 from 262,144 bodies on (each lane of a
@@ -154,6 +162,16 @@ nbgb_status nbgb_calculator_create(nbgb_method method, const nbgb_params* params
 nbgb_status nbgb_calculator_destroy(nbgb_calculator* calc);
 nbgb_status nbgb_calculator_set_params(nbgb_calculator* calc, const nbgb_params* params);
 nbgb_status nbgb_calculator_get_params(const nbgb_calculator* calc, nbgb_params* params);
+/* Device time per stage of the force evaluations made with
+ * NBGB_FLAG_STAGE_TIMINGS since it was set or since the last reset: waits for
+ * the calculator's stream, then fills up to `capacity` entries -- stage name
+ * (NUL-terminated, in names + 32 * i), total milliseconds, number of times
+ * the stage ran -- and sets *count to the number of stages (which may exceed
+ * capacity).  reset != 0 clears the totals afterwards.  No reference
+ * counterpart (its phase timer measures host enqueue time). */
+nbgb_status nbgb_calculator_stage_times(nbgb_calculator* calc, int32_t capacity, char* names,
+                                        double* total_ms, int64_t* samples, int32_t* count,
+                                        int32_t reset);
 /* ForceCalculator::getMethod (force_calculator.hpp:13) */
 nbgb_status nbgb_calculator_get_method(const nbgb_calculator* calc, nbgb_method* method);
 /* All work of the calculator is enqueued on this stream (NULL: a stream the
@@ -492,6 +510,13 @@ nbgb_status nbgb_measure_fp32_peak(double* ffma_tflops, double* ffma2_tflops, do
  * NBGB_ERR_DEVICE_TIMEOUT with the device error bits in *error_bits; the
  * context stays usable.  Nothing faults, traps or hangs. */
 nbgb_status nbgb_selftest_wait_timeout(uint32_t max_iters, uint32_t* error_bits);
+
+/* Failure injection on the host (no reference counterpart): the nth device
+ * allocation the library makes from now on (nth >= 1; 0 switches it off)
+ * fails as if the device were out of memory -- the call that needed it
+ * returns NBGB_ERR_OOM with its message and nothing is left half-built that
+ * a later call would trip over.  Process-wide; nothing reaches the GPU. */
+nbgb_status nbgb_selftest_fail_allocation(int32_t nth);
 
 /* Test hook for the Barnes-Hut group walk: the number of shared-memory stack
  * entries (64 .. 512, default 512) a warp uses before it spills the older

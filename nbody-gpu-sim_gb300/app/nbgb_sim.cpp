@@ -373,6 +373,7 @@ int run_benchmark(const Options& o) {
   p.cell_size = o.cell_size;
   p.cutoff = o.cutoff;
   if (o.group_walk && s.force_method == NBGB_BARNES_HUT) p.flags |= NBGB_FLAG_GROUP_WALK;
+  p.flags |= NBGB_FLAG_STAGE_TIMINGS;  // device time per stage, for phase_timings
   nbgb_calculator* calc = nullptr;
   check(nbgb_calculator_create((nbgb_method)s.force_method, &p, &calc));
   nbgb_system* sys = nullptr;
@@ -382,9 +383,21 @@ int run_benchmark(const Options& o) {
     nbgb_calculator_destroy(calc);
     check(st);
   }
+  // the initial force evaluation is not part of the steps: its stages are
+  // dropped from the totals
+  int32_t n_stages = 0;
+  if (st == NBGB_OK) st = nbgb_calculator_stage_times(calc, 0, nullptr, nullptr, nullptr, &n_stages, 1);
   const auto t0 = std::chrono::steady_clock::now();
-  st = nbgb_system_step(sys, s.dt, (int32_t)o.benchmark_steps);
+  if (st == NBGB_OK) st = nbgb_system_step(sys, s.dt, (int32_t)o.benchmark_steps);
   const auto t1 = std::chrono::steady_clock::now();
+  // device time per stage of the steps' force evaluations (CUDA events)
+  constexpr int kMaxStages = 32;
+  char stage_names[32 * kMaxStages] = {};
+  double stage_ms[kMaxStages] = {};
+  int64_t stage_runs[kMaxStages] = {};
+  if (st == NBGB_OK)
+    st = nbgb_calculator_stage_times(calc, kMaxStages, stage_names, stage_ms, stage_runs,
+                                     &n_stages, 0);
   if (st == NBGB_OK) {
     for (size_t k = 0; k < o.benchmark_steps; ++k) s.simulation_time += s.dt;
     if (!o.export_path.empty()) st = nbgb_system_read(sys, &h);
@@ -424,7 +437,11 @@ int run_benchmark(const Options& o) {
   out << ",\"parameters\":";
   number_map(out, params);
   out << ",\"phase_timings\":[{\"name\":\"simulation.update\",\"total_duration_ms\":" << ms
-      << ",\"samples\":" << o.benchmark_steps << "}]";
+      << ",\"samples\":" << o.benchmark_steps << "}";
+  for (int32_t i = 0; i < std::min(n_stages, kMaxStages); ++i)
+    out << ",{\"name\":\"" << (stage_names + 32 * i) << "\",\"total_duration_ms\":"
+        << stage_ms[i] << ",\"samples\":" << stage_runs[i] << "}";
+  out << "]";
   out << "}]}";
   std::cout << out.str() << std::endl;
   if (!o.benchmark_output_path.empty()) {

@@ -137,8 +137,11 @@ static void direct_forces(nbgb_calculator* c, const float4* pm, int64_t n, float
 void forces_packed(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float* ay,
                    float* az) {
   if (n <= 0) return;
+  StageTimer* t = stage_timer(c);
+  if (t) t->st = c->stream;
   switch (c->method) {
     case NBGB_DIRECT_N2:
+      stage_mark(t, "direct.forces");
       direct_forces(c, pm, n, ax, ay, az);
       break;
     case NBGB_BARNES_HUT:
@@ -148,6 +151,71 @@ void forces_packed(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, f
       hash_forces(c, pm, n, ax, ay, az);
       break;
   }
+  if (t) t->end();
+}
+
+// ------------------------------------------------------- stage timings --
+StageTimer::~StageTimer() {
+  for (auto& m : marks) cudaEventDestroy(m.ev);
+  for (auto e : spare) cudaEventDestroy(e);
+}
+
+int StageTimer::id_of(const char* name) {
+  for (size_t i = 0; i < names.size(); ++i)
+    if (names[i] == name) return (int)i;
+  names.emplace_back(name);
+  total_ms.push_back(0.0);
+  samples.push_back(0);
+  return (int)names.size() - 1;
+}
+
+cudaEvent_t StageTimer::record(int stage) {
+  cudaEvent_t ev = nullptr;
+  if (!spare.empty()) {
+    ev = spare.back();
+    spare.pop_back();
+  } else {
+    NBGB_CUDA(cudaEventCreate(&ev));
+  }
+  marks.push_back(Mark{stage, ev});
+  NBGB_CUDA(cudaEventRecord(ev, st));
+  return ev;
+}
+
+void StageTimer::mark(const char* stage) {
+  if (marks.size() > 4096) harvest();  // bounds the events held between queries
+  record(id_of(stage));
+}
+
+void StageTimer::end() {
+  if (!marks.empty() && marks.back().stage >= 0) record(-1);
+}
+
+void StageTimer::harvest() {
+  if (marks.empty()) return;
+  NBGB_CUDA(cudaEventSynchronize(marks.back().ev));
+  const size_t last = marks.size() - 1;
+  for (size_t i = 0; i < last; ++i) {
+    if (marks[i].stage < 0) continue;
+    float ms = 0.f;
+    NBGB_CUDA(cudaEventElapsedTime(&ms, marks[i].ev, marks[i + 1].ev));
+    total_ms[(size_t)marks[i].stage] += ms;
+    samples[(size_t)marks[i].stage] += 1;
+  }
+  // a stage that began at the last mark is still open: keep that mark
+  const bool open = marks[last].stage >= 0;
+  for (size_t i = 0; i < (open ? last : last + 1); ++i) spare.push_back(marks[i].ev);
+  if (open) {
+    const Mark keep = marks[last];
+    marks.assign(1, keep);
+  } else {
+    marks.clear();
+  }
+}
+
+void StageTimer::reset() {
+  std::fill(total_ms.begin(), total_ms.end(), 0.0);
+  std::fill(samples.begin(), samples.end(), 0);
 }
 
 static DirectVariant default_variant() {
@@ -246,6 +314,7 @@ nbgb_status nbgb_calculator_create(nbgb_method method, const nbgb_params* params
     auto c = std::make_unique<nbgb_calculator>();
     c->method = method;
     c->params = p;
+    if (p.flags & NBGB_FLAG_STAGE_TIMINGS) c->timer = std::make_unique<StageTimer>();
     c->variant = default_variant();
     NBGB_CUDA(cudaGetDevice(&c->device));
     NBGB_CUDA(cudaStreamCreate(&c->stream));
@@ -270,6 +339,30 @@ nbgb_status nbgb_calculator_set_params(nbgb_calculator* calc, const nbgb_params*
     if (!calc || !params) fail(NBGB_ERR_INVALID_ARG, "Validation Error: null argument");
     validate_params(calc->method, *params);
     calc->params = *params;
+    if ((params->flags & NBGB_FLAG_STAGE_TIMINGS) && !calc->timer)
+      calc->timer = std::make_unique<StageTimer>();
+  });
+}
+
+nbgb_status nbgb_calculator_stage_times(nbgb_calculator* calc, int32_t capacity, char* names,
+                                        double* total_ms, int64_t* samples, int32_t* count,
+                                        int32_t reset) {
+  return guarded([&] {
+    if (!calc || capacity < 0 || (capacity > 0 && (!names || !total_ms || !samples)))
+      fail(NBGB_ERR_INVALID_ARG, "Validation Error: null argument");
+    StageTimer* t = calc->timer.get();
+    int32_t k = 0;
+    if (t) {
+      t->harvest();
+      k = (int32_t)t->names.size();
+      for (int32_t i = 0; i < std::min(k, capacity); ++i) {
+        std::snprintf(names + 32 * (size_t)i, 32, "%s", t->names[(size_t)i].c_str());
+        total_ms[i] = t->total_ms[(size_t)i];
+        samples[i] = t->samples[(size_t)i];
+      }
+      if (reset) t->reset();
+    }
+    if (count) *count = k;
   });
 }
 
@@ -426,7 +519,7 @@ nbgb_status nbgb_particles_alloc_device(nbgb_particle_data* d, size_t count) {
     float** f = fields(d);
     const size_t bytes = std::max<size_t>(count, 1) * sizeof(float);
     for (int k = 0; k < 13; ++k) {
-      cudaError_t e = cudaMalloc(&f[k], bytes);
+      cudaError_t e = alloc_fault_injected() ? cudaErrorMemoryAllocation : cudaMalloc(&f[k], bytes);
       if (e != cudaSuccess) {
         cudaGetLastError();
         for (int j = 0; j < k; ++j) cudaFree(f[j]);

@@ -1111,7 +1111,11 @@ void bh_set_segments(BHState& h, const int64_t* off, const int64_t* n_per, int n
 // Builds the trees of all segments (positions and masses read from `pm` at
 // each segment's offset).
 void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups,
-              int group_max, bool ref_tree) {
+              int group_max, bool ref_tree, StageTimer* timer) {
+  stage_mark(timer, "barnes_hut.bounds");
+  h.built = false;  // until every kernel of this build is enqueued
+  h.groups_ready = false;
+  h.keys_valid = false;
   const int64_t n = h.n;
   const int nseg = h.nseg;
   const size_t R = (size_t)h.reserve;  // per-body buffers are sized for the reserve
@@ -1133,12 +1137,15 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   u64* lo = grow(h.klo, R);
   uint32_t* pb = grow(h.pidx, R);
   uint32_t* pb2 = grow(h.pidx_alt, R);
+  stage_mark(timer, "barnes_hut.keys");
   path_hi_index_kernel<<<grid1d(n), 256, 0, st>>>(pm, sv, n, hi, pb);
   NBGB_LAUNCH_CHECK();
+  stage_mark(timer, "barnes_hut.sort");
   bool alt = false;
   radix_sort_pairs<u64>(hi, hi2, pb, pb2, n, 0, 64, hist, sws, st, &alt, err);
   uint32_t* body = alt ? pb2 : pb;
   uint32_t* body_other = alt ? pb : pb2;
+  stage_mark(timer, "barnes_hut.order");
   if (nseg > 1) {
     // stable sort by segment: (segment, path) order
     uint32_t* sk = grow(h.sk, R);
@@ -1165,6 +1172,7 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
       fail(NBGB_ERR_INVALID_ARG,
            "Validation Error: the reference tree takes one system of at most 65536 bodies");
     // insertion order: the reference's Morton keys, stably sorted (:308-328)
+    stage_mark(timer, "barnes_hut.reference_tree");
     uint32_t* mk = grow(h.mkeys, R);
     uint32_t* mi = grow(h.midx, R);
     uint32_t* mk2 = grow(h.mkeys_alt, R);
@@ -1195,9 +1203,11 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
     ref_tree_kernel<<<1, 1, 0, st>>>(ra);
     NBGB_LAUNCH_CHECK();
     h.groups_ready = false;
+    h.built = true;
     return;
   }
   // 3.-4. node counts, numbering, emission
+  stage_mark(timer, "barnes_hut.nodes");
   uint8_t* lcp = grow(h.lcp, R);
   uint32_t* cnt = grow(h.ncnt, R + 1);
   uint32_t* nst = grow(h.nstart, R + 1);
@@ -1240,9 +1250,11 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   // tree, so bodies are not chained per thread (one resident wave of threads
   // striding over the node slots was 0.3 ms per serving tick slower); blocks
   // of two warps, so that a block waiting for one long climb holds few slots
+  stage_mark(timer, "barnes_hut.com");
   com_kernel<<<(unsigned)ceil_div(std::max<int64_t>(n, 1), kComThreads), kComThreads, 0, st>>>(
       nodes, spm, nst, n, h.cap, par, nch, vis, leaf_of);
   NBGB_LAUNCH_CHECK();
+  h.built = true;
 }
 
 // Resident 256-thread blocks per SM of one walk instantiation.
@@ -1312,6 +1324,54 @@ void bh_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, float* az,
 // Node capacity that any realistic input fits (the canonical tree has ~1.5N
 // nodes; 4N + 64 per segment leaves room for strongly clustered sets).  Used
 // when there is no per-call synchronization (no read-back to regrow).
+// Every buffer a canonical build (and its walk) of the current segment set
+// uses, allocated ahead: bh_build then allocates nothing.  The ensemble calls
+// this before it changes any state in a tick, so that running out of device
+// memory aborts the tick cleanly instead of half-way through a step.
+void bh_reserve_buffers(BHState& h, bool groups) {
+  const int64_t n = h.n;
+  const int nseg = std::max(h.nseg, 1);
+  const size_t R = (size_t)h.reserve;
+  const int64_t min_cap = 2 * n + 64 * (int64_t)nseg;
+  if (h.cap < min_cap) h.cap = 3 * n + 64 * (int64_t)nseg;
+  if (h.cap >= kMaxWalkNodes)
+    fail(NBGB_ERR_OVERFLOW, "Barnes-Hut node capacity above 2^30 nodes: too many bodies in one tree build");
+  grow(h.box, (size_t)nseg);
+  grow(h.seg_minmax, (size_t)nseg * 6);
+  grow(h.hist, radix_hist_elems((int64_t)R));
+  grow(h.scan_ws, scan_workspace_elems((int64_t)radix_hist_elems((int64_t)R)) +
+                      scan_workspace_elems((int64_t)R + 1));
+  grow(h.khi, R);
+  grow(h.khi_alt, R);
+  grow(h.klo, R);
+  grow(h.pidx, R);
+  grow(h.pidx_alt, R);
+  if (nseg > 1) {
+    grow(h.sk, R);
+    grow(h.sk_alt, R);
+  }
+  grow(h.kseg, R);
+  grow(h.spm, R);
+  grow(h.lcp, R);
+  grow(h.ncnt, R + 1);
+  grow(h.nstart, R + 1);
+  grow(h.scalars, 2);
+  grow(h.seg_depth, (size_t)nseg);
+  grow(h.nodes, (size_t)h.cap);
+  grow(h.node_parent, (size_t)h.cap);
+  grow(h.node_nchild, (size_t)h.cap);
+  grow(h.node_visit, (size_t)h.cap);
+  grow(h.leaf_of, R);
+  grow(h.seg_root, (size_t)nseg);
+  grow(h.seg_end, (size_t)nseg);
+  grow(h.walk_ctr, 1);
+  if (groups) {
+    grow(h.groups, R);
+    grow(h.group_ctr, sizeof(GroupCounters));
+    grow(h.group_ovf, (size_t)kOvfChunks * kOvfChunk);
+  }
+}
+
 void bh_reserve_async(BHState& h) {
   const int64_t c = 4 * h.reserve + 64 * (int64_t)std::max(h.nseg, 1);
   if (h.cap < c) h.cap = std::max(c, h.cap + h.cap / 2);
@@ -1330,11 +1390,12 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
   const bool sync = (c->params.flags & NBGB_FLAG_SYNC) != 0;
   const bool ref_tree = (c->params.flags & NBGB_FLAG_REFERENCE_TREE) != 0;
   const bool groups = (c->params.flags & NBGB_FLAG_GROUP_WALK) != 0;
+  StageTimer* timer = stage_timer(c);
   if (!sync) bh_reserve_async(h);
   for (int attempt = 0; attempt < 2; ++attempt) {
     // asynchronously the reference's tree is always replayed; synchronously
     // the canonical tree is built first and replaced only where it can differ
-    bh_build(h, pm, st, err, groups, c->params.group_size, ref_tree && !sync);
+    bh_build(h, pm, st, err, groups, c->params.group_size, ref_tree && !sync, timer);
     if (!sync) break;  // capacity overflow surfaces through the device error word
     // The node count is data dependent: read it back and regrow once if the
     // capacity was too small (the kernels skipped their work in that case).
@@ -1347,7 +1408,7 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
       // count when the budget never fires, so a canonical count below
       // 2N - 33 proves that it never fires and the trees are the same.
       if (ref_tree && (int64_t)hs[0] + kMaxDepth + 1 >= 2 * n)
-        bh_build(h, pm, st, err, groups, c->params.group_size, true);
+        bh_build(h, pm, st, err, groups, c->params.group_size, true, timer);
       break;
     }
     NBGB_CUDA(cudaMemsetAsync(err, 0, sizeof(uint32_t), st));
@@ -1356,7 +1417,9 @@ void bh_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, float
   BHWalkParams wp{c->params.G, c->params.softening, c->params.theta, c->params.leaf_capacity,
                   (c->params.flags & NBGB_FLAG_GROUP_WALK) ? 1 : 0};
   const bool count = (c->params.flags & NBGB_FLAG_COUNT_INTERACTIONS) != 0;
-  bh_walk(h, wp, ax, ay, az, count ? c->counts.ensure((size_t)n) : nullptr, nullptr, err, st);
+  int32_t* counts = count ? c->counts.ensure((size_t)n) : nullptr;
+  stage_mark(timer, "barnes_hut.walk");
+  bh_walk(h, wp, ax, ay, az, counts, nullptr, err, st);
 }
 
 // ------------------------------------------------------------- export --
@@ -1406,7 +1469,7 @@ using namespace nbgb;
 extern "C" {
 
 nbgb_status nbgb_bh_tree_stats(nbgb_calculator* c, int32_t* node_count, int32_t* max_depth) {
-  if (!c || !c->bh || c->method != NBGB_BARNES_HUT) return NBGB_ERR_INVALID_ARG;
+  if (!c || !c->bh || c->method != NBGB_BARNES_HUT || !c->bh->built) return NBGB_ERR_INVALID_ARG;
   BHState& h = *c->bh;
   uint32_t total = 0;
   int32_t depth = 0;
@@ -1421,7 +1484,7 @@ nbgb_status nbgb_bh_tree_stats(nbgb_calculator* c, int32_t* node_count, int32_t*
 
 nbgb_status nbgb_bh_copy_sorted_keys(nbgb_calculator* c, uint32_t* keys, int32_t* indices,
                                      size_t n) {
-  if (!c || !c->bh || c->method != NBGB_BARNES_HUT) return NBGB_ERR_INVALID_ARG;
+  if (!c || !c->bh || c->method != NBGB_BARNES_HUT || !c->bh->built) return NBGB_ERR_INVALID_ARG;
   BHState& h = *c->bh;
   if (n != (size_t)h.n || h.nseg != 1) return NBGB_ERR_INVALID_ARG;
   if (!h.keys_valid) {
@@ -1454,7 +1517,8 @@ nbgb_status nbgb_bh_copy_sorted_keys(nbgb_calculator* c, uint32_t* keys, int32_t
 }
 
 nbgb_status nbgb_bh_copy_nodes(nbgb_calculator* c, nbgb_octree_node* nodes, size_t capacity) {
-  if (!c || !c->bh || c->method != NBGB_BARNES_HUT || !nodes) return NBGB_ERR_INVALID_ARG;
+  if (!c || !c->bh || c->method != NBGB_BARNES_HUT || !nodes || !c->bh->built)
+    return NBGB_ERR_INVALID_ARG;
   BHState& h = *c->bh;
   uint32_t total32 = 0;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return NBGB_ERR_CUDA;

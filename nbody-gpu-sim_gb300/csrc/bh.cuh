@@ -7,6 +7,7 @@
 namespace nbgb {
 
 struct BHState;
+struct StageTimer;
 
 // 32 consecutive path-sorted targets of one segment, walked by one warp.
 struct WarpTask {
@@ -43,14 +44,17 @@ void bh_set_segments(BHState& h, const int64_t* off, const int64_t* n_per, int n
                      cudaStream_t st, char* staging);
 // Node capacity for use without a read-back (4 nodes per body + 64 per segment).
 void bh_reserve_async(BHState& h);
+// Allocates every buffer bh_build / bh_walk of the current segments needs.
+void bh_reserve_buffers(BHState& h, bool groups);
 // Trees of all segments (bit-identical, per segment, to the single-system tree);
 // `groups` also emits the group walk's groups.
 // groups: emit the group walk's groups, of at most group_max bodies (32 or
 // 64; 0 = by the body count, bh_group_max).
 // ref_tree: the reference's insertion tree (node budget included) instead of
 // the canonical one; one segment of at most 65,536 bodies, no groups.
+// timer: stage marks for NBGB_FLAG_STAGE_TIMINGS (or null).
 void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool groups,
-              int group_max = 0, bool ref_tree = false);
+              int group_max = 0, bool ref_tree = false, StageTimer* timer = nullptr);
 // Accelerations of all segments, written at each segment's offset into
 // ax/ay/az.  counts (per arena index) and inter_total (running sum) are
 // optional; err receives device error bits (group walk stack overflow).

@@ -90,6 +90,7 @@ struct BHState {
   bool m_alt = false;       // Morton result in *_alt
   bool keys_valid = false;  // Morton (key, index) pairs computed for the last build
   const uint32_t* body = nullptr;  // path-sorted concatenated body indices
+  bool built = false;  // the last build finished (the inspection calls read its buffers)
 };
 
 struct SegView {

@@ -492,7 +492,6 @@ static void bh_tables(nbgb_ensemble* e) {
     }
   e->bh_n = 0;
   for (int64_t c : cnt) e->bh_n += c;
-  e->bh_dirty = false;
   e->bh_stable = 0;
   if (e->bh_exec) {
     cudaGraphExecDestroy(e->bh_exec);
@@ -509,6 +508,7 @@ static void bh_tables(nbgb_ensemble* e) {
   bh_set_segments(*e->bh, off.data(), cnt.data(), nseg, e->bh_stream, stg);
   e->up_bh.mark(e->bh_stream);
   bh_reserve_async(*e->bh);
+  e->bh_dirty = false;  // only once the new tables are in place
 }
 
 static void harvest_walk(nbgb_ensemble* e, int k) {
@@ -609,11 +609,25 @@ static void admit_batch(nbgb_ensemble* e) {
   }
   if (batch.empty()) return;
   // one staging upload; the pinned buffer is reused only after the previous
-  // upload has landed
-  if (e->stage_evt) NBGB_CUDA(cudaEventSynchronize(e->stage_evt));
-  float* hs = e->h_stage.ensure(stage_total);
+  // upload has landed.  If the staging memory cannot be had, the requests go
+  // back to the front of the queue and their arena space and slots are
+  // returned, as if this tick had not admitted them.
+  float* hs = nullptr;
+  float* ds = nullptr;
+  try {
+    if (e->stage_evt) NBGB_CUDA(cudaEventSynchronize(e->stage_evt));
+    hs = e->h_stage.ensure(stage_total);
+    ds = e->stage.ensure(stage_total);
+  } catch (...) {
+    for (auto it = batch.rbegin(); it != batch.rend(); ++it) {
+      arena_free(e, it->s->off, it->s->n_pad);
+      e->bytes_reserved -= it->s->bytes;
+      e->free_slots.push_back(it->s->slot);
+      e->queue.push_front(std::move(it->r));
+    }
+    throw;
+  }
   for (auto& p : batch) std::copy(p.r.state.begin(), p.r.state.end(), hs + p.stage_off);
-  float* ds = e->stage.ensure(stage_total);
   NBGB_CUDA(cudaMemcpyAsync(ds, hs, stage_total * sizeof(float), cudaMemcpyHostToDevice, e->main));
   if (!e->stage_evt) NBGB_CUDA(cudaEventCreateWithFlags(&e->stage_evt, cudaEventDisableTiming));
   NBGB_CUDA(cudaEventRecord(e->stage_evt, e->main));
@@ -769,6 +783,10 @@ static void run_tick(nbgb_ensemble* e) {
                                         (double)s->dt};
   SlotParams* dsp = e->d_slot.ensure((size_t)std::max(e->n_slots, 1));
   e->up_slot.upload(dsp, (size_t)e->n_slots * sizeof(SlotParams), e->main);
+  // every device buffer the rest of the tick needs is allocated before the
+  // first kernel that changes a system's state: running out of memory ends
+  // the tick here, and the next tick repeats it from the same state
+  if (e->bh_n > 0 && !e->bh_exec) bh_reserve_buffers(*e->bh, e->cfg.group_walk != 0);
   // 1. kick-drift for everything resident
   if (e->n_kd) {
     const unsigned blocks = (unsigned)std::min(e->n_kd, num_sms() * 16);

@@ -48,6 +48,7 @@ struct HashState {
   float cell = 0.f;
   int64_t total = 0;
   bool in_alt = false;
+  bool built = false;  // the last build finished (the inspection calls read its buffers)
   const uint32_t* sorted_cells() const { return in_alt ? keys_alt.ptr : keys.ptr; }
   const uint32_t* sorted_idx() const { return in_alt ? vals_alt.ptr : vals.ptr; }
 };
@@ -170,6 +171,9 @@ void hash_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, flo
                  float* az) {
   if (!c->hash) c->hash.reset(new HashState());
   HashState& h = *c->hash;
+  h.built = false;
+  StageTimer* timer = stage_timer(c);
+  stage_mark(timer, "spatial_hash.bounds");
   cudaStream_t st = c->stream;
   uint32_t* err = c->err.ensure(1);
   // 1. bounding box -> host (sizes the grid)
@@ -203,6 +207,7 @@ void hash_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, flo
     h.bmin[a] = g.bmin[a];
   }
   // 2. assign cells
+  stage_mark(timer, "spatial_hash.assign");
   int32_t* pc = h.particle_cell.ensure((size_t)n);
   uint32_t* keys = h.keys.ensure((size_t)n);
   uint32_t* vals = h.vals.ensure((size_t)n);
@@ -211,6 +216,7 @@ void hash_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, flo
   hash_assign_kernel<<<grid1d(n), 256, 0, st>>>(pm, n, g, pc, keys, vals);
   NBGB_LAUNCH_CHECK();
   // 3. stable sort by cell id
+  stage_mark(timer, "spatial_hash.sort");
   int bits = 1;
   while (bits < 32 && ((int64_t)1 << bits) < total) ++bits;
   const int end_bit = ((bits + 7) / 8) * 8;
@@ -220,6 +226,7 @@ void hash_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, flo
   radix_sort_pairs<uint32_t>(keys, keys_alt, vals, vals_alt, n, 0, end_bit, hist, sws, st,
                              &h.in_alt, c->err.ensure(1));
   // 4. cell starts
+  stage_mark(timer, "spatial_hash.cells");
   uint32_t* start = h.cell_start.ensure((size_t)total + 1);
   hash_cell_start_kernel<<<grid1d(total + 1), 256, 0, st>>>(h.sorted_cells(), n, total, start);
   NBGB_LAUNCH_CHECK();
@@ -228,6 +235,7 @@ void hash_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, flo
   hash_gather_kernel<<<grid1d(n), 256, 0, st>>>(pm, h.sorted_idx(), n, spm);
   NBGB_LAUNCH_CHECK();
   // 6. cutoff gather
+  stage_mark(timer, "spatial_hash.forces");
   const float eps = c->params.softening, rc = c->params.cutoff;
   const bool count = (c->params.flags & NBGB_FLAG_COUNT_INTERACTIONS) != 0;
   int32_t* counts = count ? c->counts.ensure((size_t)n) : nullptr;
@@ -240,6 +248,7 @@ void hash_forces(nbgb_calculator* c, const float4* pm, int64_t n, float* ax, flo
                                                           start, n, g, rc * rc, eps * eps,
                                                           c->params.G, ax, ay, az, counts);
   NBGB_LAUNCH_CHECK();
+  h.built = true;
 }
 
 }  // namespace nbgb
@@ -250,7 +259,8 @@ extern "C" {
 
 nbgb_status nbgb_hash_grid_info(nbgb_calculator* c, int32_t dims[3], float bbox_min[3],
                                 float* cell_size, int64_t* total_cells) {
-  if (!c || !c->hash || c->method != NBGB_SPATIAL_HASH) return NBGB_ERR_INVALID_ARG;
+  if (!c || !c->hash || c->method != NBGB_SPATIAL_HASH || !c->hash->built)
+    return NBGB_ERR_INVALID_ARG;
   const HashState& h = *c->hash;
   for (int a = 0; a < 3; ++a) {
     if (dims) dims[a] = h.dims[a];
@@ -263,7 +273,8 @@ nbgb_status nbgb_hash_grid_info(nbgb_calculator* c, int32_t dims[3], float bbox_
 
 nbgb_status nbgb_hash_copy_cells(nbgb_calculator* c, int32_t* cell_start, int32_t* cell_end,
                                  int32_t* particle_cells, int32_t* sorted_indices) {
-  if (!c || !c->hash || c->method != NBGB_SPATIAL_HASH) return NBGB_ERR_INVALID_ARG;
+  if (!c || !c->hash || c->method != NBGB_SPATIAL_HASH || !c->hash->built)
+    return NBGB_ERR_INVALID_ARG;
   HashState& h = *c->hash;
   if (cudaStreamSynchronize(c->stream) != cudaSuccess) return NBGB_ERR_CUDA;
   const size_t tot = (size_t)h.total, n = (size_t)h.n;

@@ -1,6 +1,7 @@
 // runtime.cuh -- device buffers and the internal state behind the C handles.
 #pragma once
 
+#include <atomic>
 #include <memory>
 #include <vector>
 
@@ -8,6 +9,19 @@
 #include "kernels.cuh"
 
 namespace nbgb {
+
+// Allocation-failure injection (nbgb_selftest_fail_allocation): the
+// countdown-th device allocation from now fails as if the device were out of
+// memory, without calling the allocator.  0 = off.
+extern std::atomic<int64_t> g_alloc_fault_countdown;
+
+inline bool alloc_fault_injected() {
+  int64_t c = g_alloc_fault_countdown.load(std::memory_order_relaxed);
+  while (c > 0) {
+    if (g_alloc_fault_countdown.compare_exchange_weak(c, c - 1)) return c == 1;
+  }
+  return false;
+}
 
 // Growable device allocation (contents are not preserved on growth).
 template <typename T>
@@ -27,7 +41,7 @@ struct DevBuf {
     if (n <= cap && ptr) return ptr;
     release();
     size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
-    cudaError_t e = cudaMalloc(&ptr, bytes);
+    cudaError_t e = alloc_fault_injected() ? cudaErrorMemoryAllocation : cudaMalloc(&ptr, bytes);
     if (e != cudaSuccess) {
       ptr = nullptr;
       cudaGetLastError();
@@ -63,6 +77,41 @@ struct HostPinned {
   }
 };
 
+// Per-stage device times of a calculator (NBGB_FLAG_STAGE_TIMINGS): an event
+// is recorded on the calculator's stream where each stage of a force
+// evaluation begins and where the evaluation ends; harvest() waits for the
+// last one and adds the time between consecutive events to the stage that
+// began at the first.  Events are recycled.
+struct StageTimer {
+  cudaStream_t st = nullptr;
+  std::vector<std::string> names;
+  std::vector<double> total_ms;
+  std::vector<int64_t> samples;
+  struct Mark {
+    int stage;  // -1: the end of an evaluation
+    cudaEvent_t ev;
+  };
+  std::vector<Mark> marks;
+  std::vector<cudaEvent_t> spare;
+  StageTimer() = default;
+  StageTimer(const StageTimer&) = delete;
+  StageTimer& operator=(const StageTimer&) = delete;
+  ~StageTimer();
+  void mark(const char* stage);  // begins `stage`, ending the one before
+  void end();                    // ends the evaluation's last stage
+  void harvest();
+  void reset();
+
+ private:
+  cudaEvent_t record(int stage);
+  int id_of(const char* name);
+};
+
+// Marks a stage on an optional timer.
+inline void stage_mark(StageTimer* t, const char* stage) {
+  if (t) t->mark(stage);
+}
+
 struct BHState;    // bh.cu
 struct HashState;  // hash.cu
 void bh_state_delete(BHState*);
@@ -96,6 +145,7 @@ struct nbgb_calculator {
 
   std::unique_ptr<nbgb::BHState, nbgb::BHDeleter> bh;
   std::unique_ptr<nbgb::HashState, nbgb::HashDeleter> hash;
+  std::unique_ptr<nbgb::StageTimer> timer;  // NBGB_FLAG_STAGE_TIMINGS
 };
 
 // A device-resident system (nbgb_system_*): FP64 x, v; FP32 (or FP64) a;
@@ -118,6 +168,11 @@ namespace nbgb {
 
 // Applies a system's pending half kick (v then matches x in time).
 void system_sync_velocity(nbgb_system* s);
+
+// The calculator's stage timer while NBGB_FLAG_STAGE_TIMINGS is set.
+inline StageTimer* stage_timer(nbgb_calculator* c) {
+  return (c->params.flags & NBGB_FLAG_STAGE_TIMINGS) ? c->timer.get() : nullptr;
+}
 
 // Forces on n bodies given as packed float4 `pm` (padded by the callee's own
 // requirements where needed); writes ax/ay/az (length n).  Enqueued on

@@ -1,4 +1,5 @@
-// selftest.cu -- failure-detection self-test: a bounded wait that runs out.
+// selftest.cu -- failure-detection self-tests: a bounded wait that runs out,
+// and injected device-allocation failures.
 //
 // The kernels never trap: every wait on a bulk-copy mbarrier has an
 // iteration limit, after which the waiting thread sets kErrWaitTimeout in the
@@ -45,6 +46,17 @@ extern "C" nbgb_status nbgb_selftest_wait_timeout(uint32_t max_iters, uint32_t* 
   if (h & kErrWaitTimeout)
     return set_error(NBGB_ERR_DEVICE_TIMEOUT, "device wait ran out of iterations (self-test)");
   return NBGB_OK;
+}
+
+namespace nbgb {
+std::atomic<int64_t> g_alloc_fault_countdown{0};
+}
+
+extern "C" nbgb_status nbgb_selftest_fail_allocation(int32_t nth) {
+  if (nth < 0)
+    return set_error(NBGB_ERR_INVALID_ARG, "Validation Error: allocation index must be >= 0");
+  g_alloc_fault_countdown.store(nth);
+  return set_error(NBGB_OK, std::string());
 }
 
 extern "C" nbgb_status nbgb_selftest_group_walk_stack(int32_t entries) {

@@ -83,6 +83,7 @@ FLAG_COUNT_INTERACTIONS = 0x4
 FLAG_FP64 = 0x8
 FLAG_GROUP_WALK = 0x10
 FLAG_REFERENCE_TREE = 0x20
+FLAG_STAGE_TIMINGS = 0x40
 
 _vp = C.c_void_p
 _i32p = C.POINTER(C.c_int32)
@@ -101,6 +102,9 @@ _SIGS = {
     "nbgb_calculator_get_method": (C.c_int, [_vp, C.POINTER(C.c_int)]),
     "nbgb_calculator_set_stream": (C.c_int, [_vp, _vp]),
     "nbgb_calculator_synchronize": (C.c_int, [_vp]),
+    "nbgb_calculator_stage_times": (C.c_int, [_vp, C.c_int32, C.c_char_p,
+                                              C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                              C.POINTER(C.c_int32), C.c_int32]),
     "nbgb_compute_forces": (C.c_int, [_vp, _pd]),
     "nbgb_integrate": (C.c_int, [_vp, _pd, C.c_float]),
     "nbgb_state_kick_drift": (C.c_int, [_pd, C.c_float, _vp]),
@@ -118,6 +122,7 @@ _SIGS = {
     "nbgb_init_params_default": (None, [C.POINTER(InitParams), C.c_int32]),
     "nbgb_selftest_wait_timeout": (C.c_int, [C.c_uint32, C.POINTER(C.c_uint32)]),
     "nbgb_selftest_group_walk_stack": (C.c_int, [C.c_int32]),
+    "nbgb_selftest_fail_allocation": (C.c_int, [C.c_int32]),
     "nbgb_bh_group_size": (C.c_int32, [C.c_uint64]),
     "nbgb_init_particles_device": (C.c_int, [_pd, C.POINTER(InitParams), C.c_uint64, _vp]),
     "nbgb_bh_tree_stats": (C.c_int, [_vp, _i32p, _i32p]),

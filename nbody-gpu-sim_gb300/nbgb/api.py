@@ -15,7 +15,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (FLAG_COMPENSATED, FLAG_COUNT_INTERACTIONS, FLAG_FP64, FLAG_GROUP_WALK,
-                   FLAG_REFERENCE_TREE, FLAG_SYNC, OctreeNode, Params)
+                   FLAG_REFERENCE_TREE, FLAG_STAGE_TIMINGS, FLAG_SYNC, OctreeNode, Params)
 from ._lib import ParticleDataStruct
 
 FIELDS = ("pos_x", "pos_y", "pos_z", "vel_x", "vel_y", "vel_z", "acc_x", "acc_y", "acc_z",
@@ -259,6 +259,20 @@ class ForceCalculator:
     def synchronize(self) -> None:
         check(_lib.lib().nbgb_calculator_synchronize(self.handle))
 
+    def stage_times(self, reset: bool = False) -> dict[str, tuple[float, int]]:
+        """Device milliseconds and run count per stage of the force evaluations
+        made with FLAG_STAGE_TIMINGS (nbgb_calculator_stage_times)."""
+        cap = 32
+        names = C.create_string_buffer(32 * cap)
+        ms = (C.c_double * cap)()
+        cnt = (C.c_int64 * cap)()
+        k = C.c_int32(0)
+        check(_lib.lib().nbgb_calculator_stage_times(self.handle, cap, names, ms, cnt,
+                                                     C.byref(k), int(reset)))
+        raw = names.raw
+        return {raw[32 * i:32 * i + 32].split(b"\0")[0].decode(): (ms[i], cnt[i])
+                for i in range(min(k.value, cap))}
+
     def interaction_counts(self, n: int) -> np.ndarray:
         out = np.zeros(n, np.int32)
         check(_lib.lib().nbgb_copy_interaction_counts(self.handle, out.ctypes.data, n))
@@ -488,6 +502,6 @@ __all__ = ["ForceMethod", "forceMethodToString", "ParticleData", "ParticleDataMa
            "Integrator", "System", "ValidationException", "ResourceException", "CudaException",
            "DeviceTimeout", "CapacityError", "NbodyError", "check", "default_params",
            "FLAG_SYNC", "FLAG_COMPENSATED", "FLAG_COUNT_INTERACTIONS", "FLAG_FP64", "FLAG_GROUP_WALK",
-           "FLAG_REFERENCE_TREE",
+           "FLAG_REFERENCE_TREE", "FLAG_STAGE_TIMINGS",
            "OctreeNode",
            "Params"]

@@ -49,6 +49,19 @@ def test_benchmark_json(app, tmp_path, method):
     keys = {"dt", "gravity", "softening", "particle_count"}
     keys |= {"barnes-hut": {"theta"}, "spatial-hash": {"cell_size", "cutoff_radius"}}.get(method, set())
     assert set(b["parameters"]) == keys
+    # the reference's host phase plus the device time of each force stage
+    phases = {p["name"]: p for p in b["phase_timings"]}
+    assert phases["simulation.update"]["samples"] == 5
+    stages = {"direct-n2": ["direct.forces"],
+              "barnes-hut": ["barnes_hut.bounds", "barnes_hut.keys", "barnes_hut.sort",
+                             "barnes_hut.order", "barnes_hut.nodes", "barnes_hut.com",
+                             "barnes_hut.walk"],
+              "spatial-hash": ["spatial_hash.bounds", "spatial_hash.assign", "spatial_hash.sort",
+                               "spatial_hash.cells", "spatial_hash.forces"]}[method]
+    for name in stages:
+        assert phases[name]["samples"] >= 5 and phases[name]["total_duration_ms"] > 0, name
+    device = sum(phases[n]["total_duration_ms"] for n in stages)
+    assert device <= phases["simulation.update"]["total_duration_ms"] * 1.05
 
 
 def test_export_import_roundtrip_and_trajectory(app, tmp_path, nb):

@@ -163,12 +163,19 @@ def test_reference_tree_mode_limits(nb):
         calc.set_flags(nb.FLAG_SYNC | nb.FLAG_GROUP_WALK | nb.FLAG_REFERENCE_TREE)
     calc.close()
     big = nb.ics.plummer(65537, seed=4)
+    arrays = {"pos_x": big["x"], "pos_y": big["y"], "pos_z": big["z"], "mass": big["m"]}
+    # asynchronously the replay always runs, and is limited to 65,536 bodies
     calc = nb.BarnesHutCalculator(0.5)
-    calc.set_flags(nb.FLAG_SYNC | nb.FLAG_REFERENCE_TREE)
-    with nb.ScopedParticleData(65537, {"pos_x": big["x"], "pos_y": big["y"], "pos_z": big["z"],
-                                       "mass": big["m"]}) as p:
+    calc.set_flags(nb.FLAG_REFERENCE_TREE)
+    with nb.ScopedParticleData(65537, arrays) as p:
         with pytest.raises(nb.ValidationException, match="65536"):
             calc.computeForces(p.device)
+    calc.close()
+    # synchronously it runs only where the trees can differ: not here
+    calc = nb.BarnesHutCalculator(0.5)
+    calc.set_flags(nb.FLAG_SYNC | nb.FLAG_REFERENCE_TREE)
+    with nb.ScopedParticleData(65537, arrays) as p:
+        calc.computeForces(p.device)
     calc.close()
 
 
