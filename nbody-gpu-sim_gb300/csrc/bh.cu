@@ -437,8 +437,11 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
       ++idx;
     }
     // internal nodes of depth fd..top: slots claimed here (owner = k in
-    // parent[]), filled by internal_nodes_kernel, one thread per node
+    // parent[]); their cubes are written below on the way down to k's leaf
+    // (every owned depth lies above it), the rest by internal_nodes_kernel,
+    // one thread per node
     const int n_int = max(0, top - fd + 1);
+    const uint32_t int0 = idx;
     for (int j = 0; j < n_int; ++j) a.parent[idx + j] = (int32_t)k;
     idx += n_int;
     const bool leaf_start = first || (lp < kMaxDepth);
@@ -454,6 +457,7 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
         cy = __fadd_rn(cy, (o & 2u) ? hs : -hs);
         cz = __fadd_rn(cz, (o & 4u) ? hs : -hs);
         h = hs;
+        if (lev >= fd && lev <= top) a.nodes[int0 + (lev - fd)].geom = make_float4(cx, cy, cz, h);
       }
       int64_t e = k;
       while (e + 1 < a.n && a.kseg[e + 1] == s && (int)a.lcp[e] >= kMaxDepth) ++e;
@@ -475,8 +479,9 @@ __global__ void emit_nodes_kernel(EmitArgs a) {
 }
 
 // Internal nodes, one thread per node: the owner body k (the first body of
-// the node's range) and the depth follow from k's slot numbering; the centre
-// is k's path to that depth, the range end a search over the sorted keys.
+// the node's range) and the depth follow from k's slot numbering, the range
+// end from a search over the sorted keys (the cube was written by
+// emit_nodes_kernel on k's path).
 __global__ void internal_nodes_kernel(EmitArgs a) {
   const uint32_t total = a.nstart[a.n];
   if ((int64_t)total > a.cap) return;
@@ -489,20 +494,8 @@ __global__ void internal_nodes_kernel(EmitArgs a) {
     const bool first = (k == 0) || a.kseg[k - 1] != s;
     const int fd = first ? 1 : (int)a.lcp[k - 1] + 1;
     const int d = fd + (int)(q - (int64_t)a.nstart[k]) - (first ? 1 : 0);
-    const float4 p = a.spm[k];
-    const BBox b = a.box[s];
-    float cx = b.center[0], cy = b.center[1], cz = b.center[2], h = b.half;
-    for (int lev = 1; lev <= d; ++lev) {
-      const uint32_t o = (p.x >= cx ? 1u : 0u) | (p.y >= cy ? 2u : 0u) | (p.z >= cz ? 4u : 0u);
-      const float hs = __fmul_rn(h, 0.5f);
-      cx = __fadd_rn(cx, (o & 1u) ? hs : -hs);
-      cy = __fadd_rn(cy, (o & 2u) ? hs : -hs);
-      cz = __fadd_rn(cz, (o & 4u) ? hs : -hs);
-      h = hs;
-    }
     const int64_t e = range_end(a.kseg, a.hi, a.lo, a.n, k, d);
     const uint32_t skip = (e + 1 < a.n) ? a.nstart[e + 1] : total;
-    a.nodes[q].geom = make_float4(cx, cy, cz, h);
     a.nodes[q].info = make_int4((int)skip, d << 8, (int)k, (int)(e - k + 1));
     a.visit[q] = 0;
   }
