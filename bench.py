@@ -74,6 +74,9 @@ def parse():
                          "(small profiling cases), or run the precision study")
     ap.add_argument("--case-n", type=int, default=None,
                     help="bodies of a --case run (262144; 33554432 for integrate)")
+    ap.add_argument("--stage-times", action="store_true",
+                    help="with --case: device milliseconds per stage of the timed evaluations "
+                         "(NBGB_FLAG_STAGE_TIMINGS)")
     ap.add_argument("--precision-steps", type=int, default=2000)
     ap.add_argument("--precision-fp64-steps", type=int, default=16,
                     help="steps of the three-variant run at the full N of --case precision")
@@ -128,6 +131,8 @@ def case_arm(args, local):
         calc = nbgb.BarnesHutCalculator(0.5, leaf_capacity=8 if args.case in ("bh8", "bhg8") else 1,
                                         group_walk=args.case in ("bhg", "bhg8"))
     calc.setSofteningParameter(EPS)
+    if args.stage_times:
+        calc.set_flags(calc.params.flags | nbgb.FLAG_STAGE_TIMINGS)
     st = torch.cuda.current_stream()
     calc.set_stream(st.cuda_stream)
     with nbgb.ScopedParticleData(n, {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"],
@@ -135,14 +140,20 @@ def case_arm(args, local):
         for _ in range(max(args.warmup, 1)):
             calc.computeForces(p.device)
         torch.cuda.synchronize()
+        if args.stage_times:
+            calc.stage_times(reset=True)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
         for _ in range(args.steps):
             calc.computeForces(p.device)
         e1.record(st)
         torch.cuda.synchronize()
+        stages = calc.stage_times() if args.stage_times else None
     calc.close()
-    return {"case": args.case, "n": n, "ms_per_eval": e0.elapsed_time(e1) / args.steps}
+    out = {"case": args.case, "n": n, "ms_per_eval": e0.elapsed_time(e1) / args.steps}
+    if stages:
+        out["stage_ms_per_eval"] = {k: round(v[0] / max(v[1], 1), 4) for k, v in stages.items()}
+    return out
 
 
 def per_config_timings(nbgb) -> dict:
