@@ -508,6 +508,9 @@ struct GroupSink {
   int4* groups;          // first body, count, segment
   GroupCounters* gc;
   int gmax;              // largest group (32 or 64 bodies)
+  int64_t gcap;          // groups capacity
+  const uint32_t* body_cost;           // last walk's cost per body
+  const unsigned long long* cost_acc;  // last walk's total cost, groups
 };
 
 // Parent links and child counts (children of P: P+1, skip(P+1), ... < skip(P)).
@@ -517,7 +520,10 @@ struct GroupSink {
 // kGroupMergeMax bodies: sibling cells of a large sparse node can lie far
 // apart); depth-32 leaves larger than a group are split.  Every body
 // belongs to exactly one group, and a group is one contiguous range of
-// path-sorted bodies.
+// path-sorted bodies.  Groups whose first body's group cost more than the
+// mean in the last walk go to the front of the array, the others to the
+// back, and the walk takes the front first: the longest groups start early
+// and the walk's last tasks are short ones.
 template <bool GROUPS>
 __global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __restrict__ nstart,
                             int64_t n, int64_t cap, int32_t* __restrict__ parent,
@@ -525,9 +531,14 @@ __global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __re
   const uint32_t total = nstart[n];
   if ((int64_t)total > cap) return;
   const int gmax = gs.gmax;
+  uint32_t mean = 0xffffffffu;  // no estimates before the first walk
+  if (GROUPS && gs.cost_acc[1]) mean = (uint32_t)(gs.cost_acc[0] / gs.cost_acc[1]);
   auto emit = [&](int f, int c) {
-    const uint32_t g = atomicAdd(&gs.gc->ngroups, 1u);
-    gs.groups[g] = make_int4(f, c, gs.seg_of[gs.body[f]], 0);
+    const uint32_t b = gs.body[f];
+    const uint32_t g = gs.body_cost[b] > mean
+                           ? atomicAdd(&gs.gc->nheavy, 1u)
+                           : (uint32_t)(gs.gcap - 1) - atomicAdd(&gs.gc->nlight, 1u);
+    gs.groups[g] = make_int4(f, c, gs.seg_of[b], 0);
   };
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
        p += (int64_t)gridDim.x * blockDim.x) {
@@ -1051,7 +1062,8 @@ size_t bh_state_bytes(const BHState* p) {
          h.scalars.bytes() + h.nodes.bytes() +
          h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() +
          h.leaf_of.bytes() + h.ref_nodes.bytes() + h.ref_pos.bytes() + h.spm.bytes() +
-         h.walk_ctr.bytes() + h.groups.bytes() + h.group_ctr.bytes() + h.group_ovf.bytes();
+         h.walk_ctr.bytes() + h.groups.bytes() + h.body_cost.bytes() + h.cost_acc.bytes() +
+         h.group_ctr.bytes() + h.group_ovf.bytes();
 }
 
 size_t bh_bytes_estimate(int64_t n) { return (size_t)n * 480 + (64u << 10); }
@@ -1228,11 +1240,21 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
   NBGB_LAUNCH_CHECK();
   if (groups) {
     h.group_max = group_max > 0 ? group_max : bh_group_max(n);
-    GroupSink gs{h.body, h.seg_of.ptr, grow(h.groups, R),
+    uint32_t* bc_old = h.body_cost.ptr;
+    uint32_t* bc = grow(h.body_cost, R);
+    if (bc != bc_old) NBGB_CUDA(cudaMemsetAsync(bc, 0, h.body_cost.cap * sizeof(uint32_t), st));
+    unsigned long long* acc_old = h.cost_acc.ptr;
+    unsigned long long* acc = grow(h.cost_acc, 2);
+    if (acc != acc_old) NBGB_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), st));
+    int4* gr = grow(h.groups, R);
+    GroupSink gs{h.body, h.seg_of.ptr, gr,
                  reinterpret_cast<GroupCounters*>(grow(h.group_ctr, sizeof(GroupCounters))),
-                 h.group_max};
+                 h.group_max, (int64_t)h.groups.cap, bc, acc};
     NBGB_CUDA(cudaMemsetAsync(gs.gc, 0, sizeof(GroupCounters), st));
     link_kernel<true><<<grid1d(h.cap), 256, 0, st>>>(nodes, nst, n, h.cap, par, nch, gs);
+    NBGB_LAUNCH_CHECK();
+    // the coming walk adds up its own costs
+    NBGB_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), st));
   } else {
     link_kernel<false><<<grid1d(h.cap), 256, 0, st>>>(nodes, nst, n, h.cap, par, nch, GroupSink{});
   }
@@ -1360,6 +1382,12 @@ void bh_reserve_buffers(BHState& h, bool groups) {
   grow(h.walk_ctr, 1);
   if (groups) {
     grow(h.groups, R);
+    uint32_t* bc_old = h.body_cost.ptr;
+    uint32_t* bc = grow(h.body_cost, R);
+    if (bc != bc_old) NBGB_CUDA(cudaMemset(bc, 0, h.body_cost.cap * sizeof(uint32_t)));
+    unsigned long long* acc_old = h.cost_acc.ptr;
+    unsigned long long* acc = grow(h.cost_acc, 2);
+    if (acc != acc_old) NBGB_CUDA(cudaMemset(acc, 0, 2 * sizeof(unsigned long long)));
     grow(h.group_ctr, sizeof(GroupCounters));
     grow(h.group_ovf, (size_t)kOvfChunks * kOvfChunk);
   }

@@ -49,6 +49,9 @@ struct GroupWalkArgs {
   int stack_limit;                  // shared stack entries used (64 .. kGStack)
   int leaf_cap;                     // > 1: an opened node of at most this many bodies adds
                                     // its bodies (buckets) instead of its children
+  int64_t gcap;                     // groups capacity: light groups fill it from the back
+  uint32_t* body_cost;              // out: per body, its group's cost (for the next build)
+  unsigned long long* cost_acc;     // out: total cost, groups
 };
 
 // Floats as unsigned integers with the same order (finite values).
@@ -160,14 +163,16 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
   float* ey = s_ring[wid][1];
   float* ez = s_ring[wid][2];
   float* em = s_ring[wid][3];
-  const uint32_t ngroups = *(volatile uint32_t*)&a.gc->ngroups;
+  // heavier groups (front of the array) first, then the others (back)
+  const uint32_t nheavy = *(volatile uint32_t*)&a.gc->nheavy;
+  const uint32_t ngroups = nheavy + *(volatile uint32_t*)&a.gc->nlight;
   int* ovf = nullptr;  // this warp's overflow chunk, taken on first use
   while (true) {
     uint32_t t32 = 0;
     if (lane == 0) t32 = atomicAdd(&a.gc->task, 1u);
     const uint32_t t = __shfl_sync(full, t32, 0);
     if (t >= ngroups) break;
-    const int4 g = a.groups[t];  // first, count, segment
+    const int4 g = a.groups[t < nheavy ? (int64_t)t : a.gcap - 1 - (int64_t)(t - nheavy)];
     // a group of at most 8 (16) bodies gives each body 4 (2) lanes, each
     // summing a share of the list: lane = replica * gw + body; in a group of
     // more than 32 bodies every lane sums body `lane`, and its h - 32 second
@@ -438,6 +443,15 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
       a.az[i] = a.G * (sz0 + sz1);
       if (COUNT && a.counts) a.counts[i] = cnt_lane2;
     }
+    {  // this group's cost, for the order of the next build's groups
+      const uint32_t cost = wr * (two ? 2u : 1u);
+      if (owner) a.body_cost[a.body[k]] = cost;
+      if (owner2) a.body_cost[a.body[k2]] = cost;
+      if (lane == 0) {
+        atomicAdd(&a.cost_acc[0], (unsigned long long)cost);
+        atomicAdd(&a.cost_acc[1], 1ull);
+      }
+    }
     if (CNT > 0 && a.inter_total) {
       const int own = CNT == 2 ? cnt_lane : (int)wr - (pi.w != 0.0f ? 1 : 0);
       const int own2 = CNT == 2 ? cnt_lane2 : (int)wr - (pj.w != 0.0f ? 1 : 0);
@@ -519,6 +533,9 @@ void bh_group_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, floa
   g.err = err;
   g.stack_limit = g_group_stack_limit.load();
   g.leaf_cap = p.leaf_capacity;
+  g.gcap = (int64_t)h.groups.cap;
+  g.body_cost = h.body_cost.ptr;
+  g.cost_acc = h.cost_acc.ptr;
   const int cnt = counts ? 2 : (inter_total ? 1 : 0);
   const bool zero_eps = g.eps2 == 0.0f;
   const bool two = h.group_max > 32;

@@ -79,7 +79,11 @@ struct BHState {
   DevBuf<int32_t> ref_pos;  // reference-identical build: original index -> sorted position
   DevBuf<float4> spm;      // bodies in path order
   DevBuf<uint32_t> walk_ctr;  // next warp task of the walk
-  DevBuf<int4> groups;        // group walk: first body, count, segment
+  DevBuf<int4> groups;        // group walk: first body, count, segment (heavier groups
+                              // from the front, the others from the back)
+  DevBuf<uint32_t> body_cost;  // group walk: per concatenated body, the cost of its
+                               // group in the last walk (list entries x bodies per lane)
+  DevBuf<unsigned long long> cost_acc;  // the last walk's total cost and group count
   bool groups_ready = false;  // the last build emitted groups
   int group_max = 32;           // largest group of the last build (32 or 64 bodies)
   DevBuf<char> group_ctr;     // group walk: GroupCounters
@@ -118,10 +122,10 @@ constexpr int kOvfChunks = 256;       // overflow chunks per launch
 constexpr float kBoxWiden = 0x1.000004p0f;  // 1 + 2^-22: covers the half sizes' rounding
 
 struct GroupCounters {
-  uint32_t ngroups;  // groups emitted by link_kernel
-  uint32_t task;     // next group of the walk
-  uint32_t ovf;      // overflow chunks handed out
-  uint32_t pad;
+  uint32_t nheavy;  // groups emitted at the front (estimated above the mean cost)
+  uint32_t task;    // next group of the walk
+  uint32_t ovf;     // overflow chunks handed out
+  uint32_t nlight;  // groups emitted at the back
 };
 
 // Largest group of a build over n bodies (all segments together): groups of
