@@ -505,7 +505,8 @@ __global__ void internal_nodes_kernel(EmitArgs a) {
 struct GroupSink {
   const uint32_t* body;  // path-sorted position -> concatenated body index
   const int32_t* seg_of;
-  int4* groups;          // first body, count, segment
+  int4* groups;          // first body, count, segment: classes 0 and 1
+  int4* groups2;         // classes 2 and 3
   GroupCounters* gc;
   int gmax;              // largest group (32 or 64 bodies)
   int64_t gcap;          // groups capacity
@@ -520,10 +521,11 @@ struct GroupSink {
 // kGroupMergeMax bodies: sibling cells of a large sparse node can lie far
 // apart); depth-32 leaves larger than a group are split.  Every body
 // belongs to exactly one group, and a group is one contiguous range of
-// path-sorted bodies.  Groups whose first body's group cost more than the
-// mean in the last walk go to the front of the array, the others to the
-// back, and the walk takes the front first: the longest groups start early
-// and the walk's last tasks are short ones.
+// path-sorted bodies.  Groups go to four cost classes (GroupCounters) by
+// the last walk's cost of their first body's group: classes 0 and 1 to the
+// front and back of groups, 2 and 3 to those of groups2; the walk takes
+// class 0 first, so the longest groups start early and its last tasks are
+// short ones.
 template <bool GROUPS>
 __global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __restrict__ nstart,
                             int64_t n, int64_t cap, int32_t* __restrict__ parent,
@@ -531,14 +533,16 @@ __global__ void link_kernel(const Node* __restrict__ nodes, const uint32_t* __re
   const uint32_t total = nstart[n];
   if ((int64_t)total > cap) return;
   const int gmax = gs.gmax;
-  uint32_t mean = 0xffffffffu;  // no estimates before the first walk
-  if (GROUPS && gs.cost_acc[1]) mean = (uint32_t)(gs.cost_acc[0] / gs.cost_acc[1]);
+  unsigned long long mean = ~0ull;  // no estimates before the first walk
+  if (GROUPS && gs.cost_acc[1]) mean = gs.cost_acc[0] / gs.cost_acc[1];
   auto emit = [&](int f, int c) {
     const uint32_t b = gs.body[f];
-    const uint32_t g = gs.body_cost[b] > mean
-                           ? atomicAdd(&gs.gc->nheavy, 1u)
-                           : (uint32_t)(gs.gcap - 1) - atomicAdd(&gs.gc->nlight, 1u);
-    gs.groups[g] = make_int4(f, c, gs.seg_of[b], 0);
+    const unsigned long long e = gs.body_cost[b];
+    const int cls = mean == ~0ull ? 3 : (e > 2 * mean ? 0 : (e > mean ? 1 : (2 * e > mean ? 2 : 3)));
+    const uint32_t k = atomicAdd(&gs.gc->nclass[cls], 1u);
+    int4* arr = cls < 2 ? gs.groups : gs.groups2;
+    const int64_t g = (cls & 1) ? gs.gcap - 1 - (int64_t)k : (int64_t)k;
+    arr[g] = make_int4(f, c, gs.seg_of[b], 0);
   };
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < (int64_t)total;
        p += (int64_t)gridDim.x * blockDim.x) {
@@ -1062,7 +1066,7 @@ size_t bh_state_bytes(const BHState* p) {
          h.scalars.bytes() + h.nodes.bytes() +
          h.node_parent.bytes() + h.node_nchild.bytes() + h.node_visit.bytes() +
          h.leaf_of.bytes() + h.ref_nodes.bytes() + h.ref_pos.bytes() + h.spm.bytes() +
-         h.walk_ctr.bytes() + h.groups.bytes() + h.body_cost.bytes() + h.cost_acc.bytes() +
+         h.walk_ctr.bytes() + h.groups.bytes() + h.groups2.bytes() + h.body_cost.bytes() + h.cost_acc.bytes() +
          h.group_ctr.bytes() + h.group_ovf.bytes();
 }
 
@@ -1247,7 +1251,8 @@ void bh_build(BHState& h, const float4* pm, cudaStream_t st, uint32_t* err, bool
     unsigned long long* acc = grow(h.cost_acc, 2);
     if (acc != acc_old) NBGB_CUDA(cudaMemsetAsync(acc, 0, 2 * sizeof(unsigned long long), st));
     int4* gr = grow(h.groups, R);
-    GroupSink gs{h.body, h.seg_of.ptr, gr,
+    int4* gr2 = h.groups2.ensure(h.groups.cap);
+    GroupSink gs{h.body, h.seg_of.ptr, gr, gr2,
                  reinterpret_cast<GroupCounters*>(grow(h.group_ctr, sizeof(GroupCounters))),
                  h.group_max, (int64_t)h.groups.cap, bc, acc};
     NBGB_CUDA(cudaMemsetAsync(gs.gc, 0, sizeof(GroupCounters), st));
@@ -1382,6 +1387,7 @@ void bh_reserve_buffers(BHState& h, bool groups) {
   grow(h.walk_ctr, 1);
   if (groups) {
     grow(h.groups, R);
+    h.groups2.ensure(h.groups.cap);
     uint32_t* bc_old = h.body_cost.ptr;
     uint32_t* bc = grow(h.body_cost, R);
     if (bc != bc_old) NBGB_CUDA(cudaMemset(bc, 0, h.body_cost.cap * sizeof(uint32_t)));

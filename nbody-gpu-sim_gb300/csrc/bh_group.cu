@@ -31,7 +31,8 @@ struct GroupWalkArgs {
   const uint32_t* body;
   const uint32_t* nstart;
   SegView sv;
-  const int4* groups;
+  const int4* groups;   // cost classes 0 (front) and 1 (back)
+  const int4* groups2;  // cost classes 2 (front) and 3 (back)
   const int32_t* seg_root;
   int64_t n;
   int64_t cap;
@@ -163,16 +164,21 @@ __global__ void __launch_bounds__(kGWarps * 32, TWO ? 3 : 4) bh_group_walk_kerne
   float* ey = s_ring[wid][1];
   float* ez = s_ring[wid][2];
   float* em = s_ring[wid][3];
-  // heavier groups (front of the array) first, then the others (back)
-  const uint32_t nheavy = *(volatile uint32_t*)&a.gc->nheavy;
-  const uint32_t ngroups = nheavy + *(volatile uint32_t*)&a.gc->nlight;
+  // the cost classes in order: class 0 (longest) first
+  const uint32_t c0 = *(volatile uint32_t*)&a.gc->nclass[0];
+  const uint32_t c01 = c0 + *(volatile uint32_t*)&a.gc->nclass[1];
+  const uint32_t c012 = c01 + *(volatile uint32_t*)&a.gc->nclass[2];
+  const uint32_t ngroups = c012 + *(volatile uint32_t*)&a.gc->nclass[3];
   int* ovf = nullptr;  // this warp's overflow chunk, taken on first use
   while (true) {
     uint32_t t32 = 0;
     if (lane == 0) t32 = atomicAdd(&a.gc->task, 1u);
     const uint32_t t = __shfl_sync(full, t32, 0);
     if (t >= ngroups) break;
-    const int4 g = a.groups[t < nheavy ? (int64_t)t : a.gcap - 1 - (int64_t)(t - nheavy)];
+    const int4 g = t < c0     ? a.groups[t]
+                   : t < c01  ? a.groups[a.gcap - 1 - (int64_t)(t - c0)]
+                   : t < c012 ? a.groups2[t - c01]
+                              : a.groups2[a.gcap - 1 - (int64_t)(t - c012)];
     // a group of at most 8 (16) bodies gives each body 4 (2) lanes, each
     // summing a share of the list: lane = replica * gw + body; in a group of
     // more than 32 bodies every lane sums body `lane`, and its h - 32 second
@@ -517,6 +523,7 @@ void bh_group_walk(BHState& h, const BHWalkParams& p, float* ax, float* ay, floa
   g.nstart = h.nstart.ptr;
   g.sv = SegView{h.seg_off_p, h.seg_base_p, h.seg_of.ptr, h.box.ptr};
   g.groups = groups;
+  g.groups2 = h.groups2.ptr;
   g.seg_root = h.seg_root.ptr;
   g.n = n;
   g.cap = h.cap;

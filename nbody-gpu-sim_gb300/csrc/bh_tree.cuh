@@ -79,8 +79,9 @@ struct BHState {
   DevBuf<int32_t> ref_pos;  // reference-identical build: original index -> sorted position
   DevBuf<float4> spm;      // bodies in path order
   DevBuf<uint32_t> walk_ctr;  // next warp task of the walk
-  DevBuf<int4> groups;        // group walk: first body, count, segment (heavier groups
-                              // from the front, the others from the back)
+  DevBuf<int4> groups;        // group walk: first body, count, segment; cost classes 0 / 1
+                              // from the front / back of groups, 2 / 3 of groups2
+  DevBuf<int4> groups2;
   DevBuf<uint32_t> body_cost;  // group walk: per concatenated body, the cost of its
                                // group in the last walk (list entries x bodies per lane)
   DevBuf<unsigned long long> cost_acc;  // the last walk's total cost and group count
@@ -121,11 +122,16 @@ constexpr int kOvfChunk = 8704;       // per-warp stack overflow: 32 x 8 sibling
 constexpr int kOvfChunks = 256;       // overflow chunks per launch
 constexpr float kBoxWiden = 0x1.000004p0f;  // 1 + 2^-22: covers the half sizes' rounding
 
+// Groups by their estimated cost (the last walk's cost of their first
+// body's group) against the last walk's mean: class 0 above 2x the mean,
+// 1 above the mean, 2 above half of it, 3 the rest (and groups without an
+// estimate); the walk takes the classes in that order.
+constexpr int kCostClasses = 4;
 struct GroupCounters {
-  uint32_t nheavy;  // groups emitted at the front (estimated above the mean cost)
-  uint32_t task;    // next group of the walk
-  uint32_t ovf;     // overflow chunks handed out
-  uint32_t nlight;  // groups emitted at the back
+  uint32_t nclass[kCostClasses];  // groups emitted per cost class
+  uint32_t task;                  // next group of the walk
+  uint32_t ovf;                   // overflow chunks handed out
+  uint32_t pad[2];
 };
 
 // Largest group of a build over n bodies (all segments together): groups of
