@@ -443,9 +443,9 @@ def gpu_arm(args, rank, world, local):
         direct_share = (dms / 1e3) / elapsed_s if elapsed_s > 0 else None
         # DRAM bytes of the walk: ncu capture (dram__bytes_read.sum +
         # dram__bytes_write.sum) of the group-walk launch of the first timed
-        # tick of this workload, 216.6 MB + 19.8 MB for 1,179,805 bodies
+        # tick of this workload, 341.7 MB + 36.1 MB for 1,179,805 bodies
         # walked, scaled by the bodies walked here
-        walk_traffic = 236.43e6 / 1179805 * bh_bodies if bh_bodies else None
+        walk_traffic = 377.85e6 / 1179805 * bh_bodies if bh_bodies else None
         clocks = clk.summary()
         clocks["window"] = "timed ticks and the saturated end-to-end run"
         out = {
@@ -499,7 +499,7 @@ def gpu_arm(args, rank, world, local):
                 "frac": (w_achieved / ffma_peak) if w_achieved else None,
                 "traffic": walk_traffic,
                 "traffic_source": "ncu dram__bytes_read+write of the group-walk launch of the "
-                                  "first timed tick of this workload (236.4 MB for 1,179,805 "
+                                  "first timed tick of this workload (377.9 MB for 1,179,805 "
                                   "bodies walked), scaled by the bodies walked",
                 "algorithmic_bytes": 64 * 1.5 * bh_bodies + 28 * bh_bodies if bh_bodies else None,
                 "peak_source": "measured in-process: FFMA chains on every SM "

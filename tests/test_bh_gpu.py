@@ -286,6 +286,30 @@ def test_group_walk_theta0_is_direct_sum(nb, orc):
     assert np.max(vec_rel_err(*r["acc"], bx, by, bz)) < 1e-4
 
 
+@pytest.mark.parametrize("gen,n,leaf", [("two", 300000, 1), ("plummer", 20000, 1), ("two", 50000, 8)])
+def test_group_order_does_not_change_results(nb, gen, n, leaf):
+    """The walk takes the groups in cost classes learned from the previous
+    evaluation (the first evaluation has none): repeated evaluations of the
+    same bodies give bitwise-identical accelerations and list lengths."""
+    s = _gen(nb, gen, n)
+    calc = nb.BarnesHutCalculator(0.5, leaf_capacity=leaf, group_walk=True)
+    calc.setSofteningParameter(0.01)
+    calc.set_flags(nb.FLAG_SYNC | nb.FLAG_COMPENSATED | nb.FLAG_COUNT_INTERACTIONS |
+                   nb.FLAG_GROUP_WALK)
+    runs = []
+    with nb.ScopedParticleData(n, {"pos_x": s["x"], "pos_y": s["y"], "pos_z": s["z"],
+                                   "mass": s["m"]}) as p:
+        for _ in range(3):
+            calc.computeForces(p.device)
+            p.download()
+            runs.append((p.host["acc_x"].copy(), p.host["acc_y"].copy(), p.host["acc_z"].copy(),
+                         calc.interaction_counts(n)))
+    calc.close()
+    for r in runs[1:]:
+        for a, b in zip(runs[0], r):
+            np.testing.assert_array_equal(a, b)
+
+
 def test_group_walk_is_more_accurate_than_reference_walk(nb, orc):
     # every accepted cell passes the per-target test for each body of the group
     n = 65536
