@@ -1388,12 +1388,17 @@ void bh_reserve_buffers(BHState& h, bool groups) {
   if (groups) {
     grow(h.groups, R);
     h.groups2.ensure(h.groups.cap);
+    // fresh cost estimates (zero: no order yet), complete before any stream
+    // of the caller uses them
     uint32_t* bc_old = h.body_cost.ptr;
     uint32_t* bc = grow(h.body_cost, R);
-    if (bc != bc_old) NBGB_CUDA(cudaMemset(bc, 0, h.body_cost.cap * sizeof(uint32_t)));
     unsigned long long* acc_old = h.cost_acc.ptr;
     unsigned long long* acc = grow(h.cost_acc, 2);
-    if (acc != acc_old) NBGB_CUDA(cudaMemset(acc, 0, 2 * sizeof(unsigned long long)));
+    if (bc != bc_old || acc != acc_old) {
+      NBGB_CUDA(cudaMemset(bc, 0, h.body_cost.cap * sizeof(uint32_t)));
+      NBGB_CUDA(cudaMemset(acc, 0, 2 * sizeof(unsigned long long)));
+      NBGB_CUDA(cudaDeviceSynchronize());
+    }
     grow(h.group_ctr, sizeof(GroupCounters));
     grow(h.group_ovf, (size_t)kOvfChunks * kOvfChunk);
   }
