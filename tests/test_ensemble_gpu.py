@@ -61,6 +61,17 @@ def test_same_alone_and_in_mix_bitwise(nb):
             np.testing.assert_array_equal(alone[key][1][k], mixed[key][1][k])
 
 
+def test_buckets_same_alone_and_in_mix_bitwise(nb):
+    """With 8-body buckets (the Barnes-Hut workload's leaf setting) a system's
+    trajectory is also the same alone and in the mix."""
+    sy = _systems(nb)
+    mixed, _ = _run(nb, sy, direct_config=0, hbm_budget_bytes=4 << 30, leaf_capacity=8)
+    alone, _ = _run(nb, {"b20000": sy["b20000"]}, direct_config=0, hbm_budget_bytes=4 << 30,
+                    leaf_capacity=8)
+    for k in ("x", "y", "z", "vx", "vy", "vz"):
+        np.testing.assert_array_equal(alone["b20000"][1][k], mixed["b20000"][1][k])
+
+
 def test_group_walk_same_alone_and_beside_many_bodies(nb):
     """The ensemble's groups have a fixed size, so a Barnes-Hut system's
     group walk (and trajectory) is the same alone and beside 300,000 other
@@ -106,12 +117,16 @@ def test_matches_plain_system_and_fp64_oracle(nb, orc):
         assert max(np.abs(got[k] - ref[k]).max() for k in ("vx", "vy", "vz")) <= 2e-4
 
 
-@pytest.mark.parametrize("group_walk", [0, 1])
-def test_bh_system_matches_plain_bh(nb, group_walk):
+@pytest.mark.parametrize("group_walk,leaf", [(0, 1), (1, 1), (0, 8), (1, 8)])
+def test_bh_system_matches_plain_bh(nb, group_walk, leaf):
+    """A Barnes-Hut system in the ensemble follows the plain one-system path
+    with the same walk (one body per leaf or buckets of at most 8 bodies)."""
     s = nb.ics.plummer(12000, seed=31)
-    res, _ = _run(nb, {"b": (s, 30)}, direct_config=0, group_walk=group_walk)
+    res, _ = _run(nb, {"b": (s, 30)}, direct_config=0, group_walk=group_walk,
+                  leaf_capacity=leaf)
     got = res["b"][1]
-    calc = nb.BarnesHutCalculator(0.5, group_walk=bool(group_walk), group_size=64)
+    calc = nb.BarnesHutCalculator(0.5, leaf_capacity=leaf, group_walk=bool(group_walk),
+                                  group_size=64)
     calc.setSofteningParameter(0.01)
     sysm = nb.System(calc, s)
     sysm.step(1e-3, 30)
