@@ -1,7 +1,8 @@
 // bh_group.cu -- the Barnes-Hut group walk (NBGB_FLAG_GROUP_WALK): one
-// interaction list per group of at most 32 nearby bodies, built by one warp
-// that tests 32 nodes at a time and evaluated by all its lanes.  Groups come
-// from the tree build (link_kernel in bh.cu).
+// interaction list per group of at most 32 or 64 nearby bodies, built by one
+// warp that tests 32 nodes at a time and evaluated by all its lanes.  Groups
+// come from the tree build (link_kernel in bh.cu), filed in cost classes
+// learned from the previous walk.
 #include <algorithm>
 #include <atomic>
 
